@@ -1,0 +1,297 @@
+"""Benchmark: queries/sec at recall@32 >= 0.99 on 1.2M x 100 unit vectors.
+
+Workload (one "step"): a batch of Q = 10,000 queries answered with k = 32 against a
+resident index of N = 1,200,000 base points, d = 100 (clustered synthetic data: 1,000
+Gaussian clusters, centres uniform on the sphere, sigma 0.05, L2-normalised; queries
+from the same centres with the next seed).  The base (480 MB fp32, 300 MB bf16) is
+larger than the 129 MB L2, so no flush is needed between steps.
+
+  --path tc       tensor-core exact scan (BF16 tcgen05 GEMM + fused top-candidates +
+                  FP32 re-rank)                       [default, the headline]
+  --path exact    plain FP32 SIMT exact scan (the denominator of the speed-up)
+  --path simhash  1024-bit SimHash + Hamming top-C + FP32 re-rank
+
+`value` is whole-job queries/sec with queries and results resident in HBM; `e2e` is the
+same metric through the C ABI with host (pinned) buffers, copies inside the timed
+region.  `--impl reference` times the reference's CPU brute force (a port of
+GoldStandard/goldstandard.cpp -- the reference binary is x86-only here) on the host
+cores over a bounded query sample.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "queries/sec at recall@32>=0.99 on 1.2Mx100 (TC+serving vs plain scan)"
+N_BASE, DIM, N_QUERY, K = 1_200_000, 100, 10_000, 32
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], p.get("bf16_tflops_sustained", p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_data(seed_offset: int):
+    from lshongpu_gb300 import datasets
+
+    x = datasets.clustered(N_BASE, DIM, seed=100 + seed_offset)
+    q = datasets.clustered(N_QUERY, DIM, seed=101 + seed_offset)
+    return x, q
+
+
+def build_index(L, x, path: str):
+    if path == "tc":
+        return L.Index(x, implementation=L.IMPL_TC, distanceFunc=1, options=L.make_options(candidates=64))
+    if path == "exact":
+        return L.Index(x, implementation=2, distanceFunc=1)
+    if path == "simhash":
+        return L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=1024))
+    raise SystemExit(f"unknown path {path}")
+
+
+def algorithmic(path: str, prof: dict, nq: int):
+    """(kernel, bound, work per launch, unit) for the dominant kernel of the path."""
+    if path == "tc":
+        return "tc_scan", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
+    if path == "exact":
+        return "scan_float", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
+    return "scan_bits", "hbm", N_BASE * 128 / 1e9, "GB/s"
+
+
+def run_reference_arm(args, world, rank):
+    import oracle
+
+    if rank != 0:
+        return
+    x, q = make_data(0)
+    threads = os.cpu_count() or 1
+    sample = max(threads, min(N_QUERY, 2 * threads))
+    qs = q[:sample]
+    for _ in range(max(0, min(args.warmup, 1))):
+        oracle.goldstandard(x, qs[:threads], K, threads)
+    times = []
+    for _ in range(args.steps):
+        _, _, t = oracle.goldstandard(x, qs, K, threads)
+        times.append(t)
+    per_q = sum(times) / (args.steps * sample)
+    qps = 1.0 / per_q
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_q * N_QUERY * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"exact angular k-NN, N={N_BASE}, d={DIM}, Q={N_QUERY} (timed on a {sample}-query "
+                               f"sample per step), k={K}", "global_batch": N_QUERY, "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} queries x {N_BASE} points per step, {args.steps} steps"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--path", default="tc", choices=["tc", "exact", "simhash"])
+    ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import lshongpu_gb300 as L
+
+    x, q = make_data(rank)
+    idx = build_index(L, x, args.path)
+    dev = torch.device("cuda", local)
+    qd = torch.from_numpy(q).to(dev)
+    out = torch.empty((N_QUERY, K, 2), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def step():
+        idx.query_device(qd.data_ptr(), N_QUERY, K, out.data_ptr(), stream=sh)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    launches0 = L.launch_count()
+    L.profile_enable(True)
+    L.profile_report()
+    with ClockSampler(local) as clk:
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        barrier()
+    L.profile_enable(False)
+    launches = L.launch_count() - launches0
+    prof = L.profile_report()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * N_QUERY / (ms_step / 1e3)
+
+    # e2e through the C ABI with pinned host buffers
+    qh = torch.from_numpy(q).pin_memory()
+    oh = torch.empty((N_QUERY, K, 2), dtype=torch.int32).pin_memory()
+    lib = L.lib()
+    for _ in range(2):
+        L.api.check(lib.lshg_index_query(idx.handle, qh.data_ptr(), N_QUERY, K, oh.data_ptr(), 0, sh))
+    barrier()
+    t0 = time.perf_counter()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        L.api.check(lib.lshg_index_query(idx.handle, qh.data_ptr(), N_QUERY, K, oh.data_ptr(), 0, sh))
+    f1.record(stream)
+    barrier()
+    e2e_ms = max(f0.elapsed_time(f1), (time.perf_counter() - t0) * 1e3) / args.steps
+    e2e_value = world * N_QUERY / (e2e_ms / 1e3)
+
+    hbm, bf16, bf16s, peak_kind = peaks()
+    kname, bound, work, unit = algorithmic(args.path, prof, N_QUERY)
+    cnt, kms = prof.get(kname, (0, 0.0))
+    achieved = (work / (kms / cnt / 1e3)) if cnt else None
+    if unit == "GB/s":
+        work_unit, peak = work, hbm
+    else:
+        work_unit, peak = work, bf16
+    roofline = {"bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+                "traffic": None, "kernel_ms_per_launch": (kms / cnt) if cnt else None,
+                "kernel_share": (kms / sum(v[1] for v in prof.values())) if prof else None}
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        import oracle
+
+        threads = os.cpu_count() or 1
+        res = out.cpu().numpy().view(np.int32)[:, :, 0]
+        nchk = 200
+        tids, _ = oracle.fp64_topk(x, q[:nchk], K, threads=threads)
+        rec = np.mean([len(set(res[i].tolist()) & set(tids[i].tolist())) / K for i in range(nchk)])
+        extras["recall_at_32"] = float(rec)
+        extras["recall_queries"] = nchk
+        # CPU baseline: GoldStandard port, bounded sample, all host threads
+        sample = 2 * threads
+        _, _, tcpu = oracle.goldstandard(x, q[:sample], K, threads)
+        cpu_qps = sample / tcpu
+        extras["cpu_baseline"] = {"value": cpu_qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                                  "sample": f"{sample} queries x {N_BASE} points (GoldStandard port)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16" if args.path == "tc" else ("u32" if args.path == "simhash" else "f32"),
+        "data": "synthetic",
+        "config": {"workload": f"k-NN path={args.path}: N={N_BASE}, d={DIM}, Q={N_QUERY}, k={K}, clustered unit "
+                               f"vectors (1000 clusters, sigma 0.05)", "global_batch": N_QUERY * world,
+                   "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
+        "roofline": roofline,
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERY * DIM * 4,
+                "d2h_bytes_per_step": N_QUERY * K * 8},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
+    }
+    line.update(extras)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,538 @@
+// Index build and query: the reference's host pipelines (linearScans, kernel.cu:27-55;
+// runLsh, lshFramework.cuh:313-460; runSimHashLinearScan, simHash.cu:61-144;
+// runWeightedMinHashLinearScan, weightedMinHash.cuh:345-429; runSimHashJLLinearScan,
+// simHashJL.cuh:287-330; runMemOptimizedLinearScan, memOptimizedLinearScan.cu:129-191)
+// re-expressed as one stream-ordered build that keeps base, sketches, keys and buckets
+// resident, and a query that only processes the query batch.
+//
+// The in-place preprocessing the reference applies to data and queries together
+// (normalisation, the Jaccard min shift) is recorded as a list of operations and
+// replayed on every query batch, with statistics taken from the base (and, for the
+// reference-compatible entry points, from the query batch it is built with).
+#include <algorithm>
+#include <cstring>
+
+#include "host_rng.h"
+#include "index.h"
+#include "launch_count.h"
+
+namespace lshg {
+
+int next_pow2(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+void launch_pack_bytes(const uint8_t* in, int64_t n, int sbytes, uint32_t* out, int wp, uint8_t pad, cudaStream_t s);
+size_t wmh_state_bytes();
+size_t lsh_query_smem(const LshQueryArgs& a);
+int lsh_query_grid(int nq);
+void launch_tc_scan(Index& idx, const float* q, int nq, int k, lshg_point* out, cudaStream_t s);
+void tc_prepare(Index& idx, cudaStream_t s);
+
+namespace {
+
+template <typename T>
+void upload(DevBuf<T>& b, const T* h, size_t count, cudaStream_t s) {
+  b.alloc(count, s);
+  if (count) LSHG_CUDA(cudaMemcpyAsync(b.ptr, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+void apply_op(const PrepOp& op, float* x, int64_t n, int d, cudaStream_t s) {
+  if (n <= 0 || !x) return;
+  if (op.kind == PrepOp::NORMALIZE) {
+    launch_normalize(x, n, d, s);
+  } else {
+    launch_shift_abs(x, n, d, op.dminv->ptr, s);
+  }
+}
+
+void apply_ops(const std::vector<PrepOp>& ops, float* x, int64_t n, int d, cudaStream_t s) {
+  for (const auto& op : ops) apply_op(op, x, n, d, s);
+}
+
+// Record-and-apply helpers: the op is applied to the base and the companion.
+void do_normalize(std::vector<PrepOp>& ops, float* x, int64_t n, float* comp, int nc, int d, cudaStream_t s) {
+  PrepOp op{PrepOp::NORMALIZE, {}, nullptr};
+  apply_op(op, x, n, d, s);
+  apply_op(op, comp, nc, d, s);
+  ops.push_back(op);
+}
+
+// transformData (processingUtils.cuh:12-46): shift every dimension by |min floor|,
+// min taken over base and companion, starting from 0.
+void do_shift(std::vector<PrepOp>& ops, float* x, int64_t n, float* comp, int nc, int d, cudaStream_t s) {
+  std::vector<int> zero(d, 0);
+  DevBuf<int> m;
+  upload(m, zero.data(), d, s);
+  launch_min_floor(x, n, d, m.ptr, s);
+  if (comp && nc > 0) launch_min_floor(comp, nc, d, m.ptr, s);
+  PrepOp op{PrepOp::SHIFT, std::vector<int>(d), nullptr};
+  LSHG_CUDA(cudaMemcpyAsync(op.minv.data(), m.ptr, d * sizeof(int), cudaMemcpyDeviceToHost, s));
+  LSHG_CUDA(cudaStreamSynchronize(s));
+  op.dminv = std::make_shared<DevBuf<int>>();
+  upload(*op.dminv, op.minv.data(), d, s);
+  apply_op(op, x, n, d, s);
+  apply_op(op, comp, nc, d, s);
+  ops.push_back(op);
+}
+
+// minHashPreprocessing + setupMaps (weightedMinHash.cuh:202-213, :71-90, :299-309) and the
+// sampler tables.  H seeds; onebit: words x hashBits layout.
+void wmh_prepare(WmhState& w, std::vector<PrepOp>& ops, float* x, int64_t n, float* comp, int nc, int d, int H,
+                 int onebit, int words, int hashBits, cudaStream_t s) {
+  do_shift(ops, x, n, comp, nc, d, s);
+  do_normalize(ops, x, n, comp, nc, d, s);
+  std::vector<int> zero(d, 0), bounds(d);
+  DevBuf<int> mb;
+  upload(mb, zero.data(), d, s);
+  launch_max_ceil(x, n, d, mb.ptr, s);
+  if (comp && nc > 0) launch_max_ceil(comp, nc, d, mb.ptr, s);
+  LSHG_CUDA(cudaMemcpyAsync(bounds.data(), mb.ptr, d * sizeof(int), cudaMemcpyDeviceToHost, s));
+  LSHG_CUDA(cudaStreamSynchronize(s));
+  int64_t M = 0;
+  w.h_start.assign(d, 0);
+  for (int i = 0; i < d; ++i) {
+    w.h_start[i] = (int)M;
+    M += std::max(0, bounds[i]);
+  }
+  LSHG_REQUIRE(M >= 1 && M < (1 << 24), "weighted MinHash: bad index-map size (all-zero or unnormalised data)");
+  w.h_map.assign((size_t)M, 0);
+  for (int i = 0; i < d; ++i)
+    for (int j = w.h_start[i]; j < w.h_start[i] + std::max(0, bounds[i]); ++j) w.h_map[j] = i;
+  w.M = (int)M;
+  w.H = H;
+  w.onebit = onebit;
+  w.words = words;
+  w.hashBits = hashBits;
+  w.T = 1024;
+  std::vector<int> seeds(H);
+  for (int h = 0; h < H; ++h) seeds[h] = h * 1234 + 92138;  // createSeedArr, weightedMinHash.cuh:252-262
+  std::vector<uint8_t> bm(255);
+  random_bools(255, bm.data());  // generateRandomBoolVectors(255), weightedMinHash.cuh:231-250
+  w.bitmapLen = 255;
+  upload(w.start, w.h_start.data(), d, s);
+  upload(w.map, w.h_map.data(), w.h_map.size(), s);
+  upload(w.seeds, seeds.data(), H, s);
+  upload(w.bitmap, bm.data(), bm.size(), s);
+  w.rtab.alloc((size_t)w.T * H, s);
+  w.states.alloc(wmh_state_bytes() * H, s);
+  launch_wmh_tables(w.seeds.ptr, H, w.T, w.M, w.rtab.ptr, w.states.ptr, s);
+  w.used = true;
+}
+
+void wmh_run(const WmhState& w, const float* x, int64_t n, int d, uint8_t* out8, uint32_t* out32, int* err,
+             cudaStream_t s) {
+  launch_wmh_sketch(x, n, d, w.start.ptr, w.map.ptr, w.M, w.rtab.ptr, w.states.ptr, w.H, w.T, w.onebit, w.words,
+                    w.hashBits, w.bitmap.ptr, w.bitmapLen, out8, out32, err, s);
+}
+
+int log_dim(int d) {  // crossPolyTope.cuh:95-104
+  int p = 1;
+  while (p < d) p *= 2;
+  return p;
+}
+
+void check_err_flag(int* err_dev, cudaStream_t s) {
+  int e = 0;
+  LSHG_CUDA(cudaMemcpyAsync(&e, err_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LSHG_CUDA(cudaStreamSynchronize(s));
+  if (e) throw Error(LSHG_ERR_SAMPLER_LIMIT, "weighted MinHash sampler exceeded its draw limit (zero or NaN input?)");
+}
+
+// Sketches of `rows` vectors (base or queries) for the index's sketch kind.  For packed
+// kinds the result has rows of wp words; byte sketches pad with `padbyte`.
+void make_sketch(const Index& idx, const float* v, int64_t rows, uint8_t padbyte, DevBuf<uint32_t>* packed,
+                 DevBuf<float>* fl, int* err, cudaStream_t s) {
+  const int d = idx.d;
+  switch (idx.sk_kind) {
+    case 3: {
+      DevBuf<uint32_t> raw(rows * idx.words, s);
+      launch_project(v, rows, d, idx.sk_planes.ptr, idx.words * 32, 0, 32, idx.words, raw.ptr, nullptr, s);
+      packed->alloc(rows * idx.wp, s);
+      launch_pad_words(raw.ptr, rows, idx.words, packed->ptr, idx.wp, 0u, s);
+      break;
+    }
+    case 4: {
+      DevBuf<uint8_t> raw(rows * idx.sbytes, s);
+      wmh_run(idx.wmh_sk, v, rows, d, raw.ptr, nullptr, err, s);
+      packed->alloc(rows * idx.wp, s);
+      launch_pack_bytes(raw.ptr, rows, idx.sbytes, packed->ptr, idx.wp, padbyte, s);
+      break;
+    }
+    case 5: {
+      DevBuf<uint32_t> raw(rows * idx.words, s);
+      wmh_run(idx.wmh_sk, v, rows, d, nullptr, raw.ptr, err, s);
+      packed->alloc(rows * idx.wp, s);
+      launch_pad_words(raw.ptr, rows, idx.words, packed->ptr, idx.wp, 0u, s);
+      break;
+    }
+    case 6: {
+      fl->alloc(rows * idx.sdim, s);
+      launch_project(v, rows, d, idx.sk_planes.ptr, idx.sdim, 1, 32, 0, nullptr, fl->ptr, s);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+void make_keys(const Index& idx, const float* v, int64_t rows, DevBuf<uint16_t>* keys, int* err, cudaStream_t s) {
+  const int d = idx.d;
+  keys->alloc(rows * idx.tables, s);
+  switch (idx.key_kind) {
+    case 3: {
+      DevBuf<uint32_t> raw(rows * idx.tables, s);
+      LSHG_CUDA(cudaMemsetAsync(raw.ptr, 0, raw.bytes(), s));
+      launch_project(v, rows, d, idx.key_planes.ptr, idx.tables * idx.key_bits, 0, idx.key_bits, idx.tables, raw.ptr,
+                     nullptr, s);
+      launch_u32_to_u16(raw.ptr, rows * idx.tables, keys->ptr, s);
+      break;
+    }
+    case 4: {
+      DevBuf<uint8_t> raw(rows * idx.tables, s);
+      wmh_run(idx.wmh_keys, v, rows, d, raw.ptr, nullptr, err, s);
+      DevBuf<uint32_t> wide(rows * idx.tables, s);
+      // widen u8 -> u16 through the packer: one byte per 32-bit word
+      launch_pack_bytes(raw.ptr, rows * idx.tables, 1, wide.ptr, 1, 0, s);
+      launch_u32_to_u16(wide.ptr, rows * idx.tables, keys->ptr, s);
+      break;
+    }
+    case 5: {
+      DevBuf<uint32_t> raw(rows * idx.tables, s);
+      wmh_run(idx.wmh_keys, v, rows, d, nullptr, raw.ptr, err, s);
+      launch_u32_to_u16(raw.ptr, rows * idx.tables, keys->ptr, s);
+      break;
+    }
+    case 7:
+      launch_crosspoly(v, rows, d, idx.cp_P, idx.tables, idx.cp_hashes, idx.cp_rounds, idx.cp_diag.ptr, keys->ptr, s);
+      break;
+    default:
+      throw Error(LSHG_ERR_INVALID_ARGUMENT, "invalid keysImplementation");
+  }
+}
+
+struct EventTimer {
+  cudaEvent_t a, b;
+  cudaStream_t s;
+  explicit EventTimer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double ms() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float m = 0;
+    cudaEventElapsedTime(&m, a, b);
+    cudaEventRecord(a, s);
+    return m;
+  }
+  ~EventTimer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+};
+
+}  // namespace
+
+Index::~Index() {
+  if (stream) cudaStreamSynchronize(stream);
+  x.release(); xnorm.release(); xt.release(); xs.release(); xsf.release(); xsft.release(); sk_planes.release();
+  keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
+  xbf.release(); xbf_scale.release(); qerr.release();
+  for (auto* ops : {&ops_keys, &ops_sketch})
+    for (auto& op : *ops)
+      if (op.dminv) op.dminv->release();
+  for (WmhState* w : {&wmh_sk, &wmh_keys}) {
+    w->start.release(); w->map.release(); w->seeds.release(); w->rtab.release(); w->states.release(); w->bitmap.release();
+  }
+  if (stream) cudaStreamSynchronize(stream);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& base, int64_t n, float* comp, int nc,
+                                   cudaStream_t s, double* prep_ms, double* build_ms) {
+  LSHG_REQUIRE(n >= 1 && p.d >= 1, "empty base or dimension");
+  LSHG_REQUIRE(n < (int64_t)INT_MAX, "base too large for 32-bit ids");
+  auto idx = std::make_unique<Index>();
+  Index& I = *idx;
+  I.p = p;
+  I.stream = s;
+  cudaGetDevice(&I.device);
+  I.n = n;
+  I.d = p.d;
+  I.x = std::move(base);
+  const int d = p.d;
+  const int impl = p.implementation == 1 ? 2 : p.implementation;
+  const int tqs = p.opt.thread_queue_size > 0 ? p.opt.thread_queue_size : 128;
+  int C = p.opt.candidates > 0 ? p.opt.candidates : 32 * tqs;
+  I.C = std::min(4096, std::max(32, next_pow2(C)));
+  DevBuf<int> err(1, s);
+  LSHG_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
+  I.qerr.alloc(1, s);
+  LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
+  EventTimer tm(s);
+  double prep = 0, build = 0;
+  float* X = I.x.ptr;
+
+  LSHG_REQUIRE(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8,
+               "Invalid implementation selected");
+  LSHG_REQUIRE(p.framework == 0 || p.framework == 1, "framework must be 0 (linear scan) or 1 (LSH)");
+
+  if (p.framework == 0) {
+    switch (impl) {
+      case 2:
+      case 8:
+        I.dist = p.distanceFunc;
+        LSHG_REQUIRE(I.dist >= 1 && I.dist <= 3, "Invalid operation selected for distance function");
+        if (I.dist == DIST_JACCARD) {  // memOptimizedLinearScan.cu:149-163
+          do_shift(I.ops_sketch, X, n, comp, nc, d, s);
+          do_normalize(I.ops_sketch, X, n, comp, nc, d, s);
+        }
+        break;
+      case 3:
+        I.dist = DIST_ANGULAR;  // simHash.cu:19
+        break;
+      case 4:
+      case 5:
+        I.dist = DIST_JACCARD;  // weightedMinHash.cuh:28
+        break;
+      case 6:
+        I.dist = DIST_ANGULAR;  // candidateSetScan(..., 1), sketchedDistanceScanners.cuh:168
+        do_normalize(I.ops_sketch, X, n, comp, nc, d, s);  // simHashJL.cuh:298
+        break;
+    }
+  } else {
+    I.dist = p.distanceFunc;
+    LSHG_REQUIRE(I.dist >= 1 && I.dist <= 3, "Invalid operation selected for distance function");
+    LSHG_REQUIRE(impl != 8, "the tensor-core scan is a linear scan");
+    LSHG_REQUIRE(p.tables >= 1 && p.tables <= 256, "tables must be in [1, 256]");
+    LSHG_REQUIRE(p.bucketKeyBits >= 1 && p.bucketKeyBits <= 24, "bucketKeyBits must be in [1, 24]");
+    I.tables = p.tables;
+    I.key_bits = p.bucketKeyBits;
+    I.tableSize = 1 << p.bucketKeyBits;
+    I.key_kind = p.keysImplementation;
+    switch (I.key_kind) {
+      case 3: {
+        std::vector<float> R((size_t)p.tables * d * p.bucketKeyBits);
+        random_normals((int64_t)R.size(), 1.0, R.data());
+        upload(I.key_planes, R.data(), R.size(), s);
+        break;
+      }
+      case 4:
+        LSHG_REQUIRE(I.tableSize >= 256, "byte weighted-MinHash keys need bucketKeyBits >= 8");
+        wmh_prepare(I.wmh_keys, I.ops_keys, X, n, comp, nc, d, p.tables, 0, 0, 0, s);
+        break;
+      case 5:
+        LSHG_REQUIRE(p.bucketKeyBits <= 32, "one-bit weighted-MinHash keys need bucketKeyBits <= 32");
+        wmh_prepare(I.wmh_keys, I.ops_keys, X, n, comp, nc, d, p.tables * p.bucketKeyBits, 1, p.tables,
+                    p.bucketKeyBits, s);
+        break;
+      case 7: {
+        I.cp_P = log_dim(d);
+        I.cp_hashes = p.opt.cp_hashes > 0 ? p.opt.cp_hashes : 1;
+        I.cp_rounds = p.opt.cp_rounds > 0 ? p.opt.cp_rounds : 3;
+        int64_t range = 1;
+        for (int h = 0; h < I.cp_hashes; ++h) range *= 2 * I.cp_P;
+        LSHG_REQUIRE(range <= 65536 && range <= I.tableSize,
+                     "cross-polytope key range (2P)^hashes exceeds the table size or 16 bits");
+        do_normalize(I.ops_keys, X, n, comp, nc, d, s);  // crossPolyTope.cuh:111
+        std::vector<int32_t> D((size_t)I.cp_P * p.tables * I.cp_hashes * I.cp_rounds);
+        random_plus_minus((int64_t)D.size(), D.data());
+        upload(I.cp_diag, D.data(), D.size(), s);
+        break;
+      }
+      default:
+        throw Error(LSHG_ERR_INVALID_ARGUMENT, "Invalid implementation selected for LSH.");
+    }
+  }
+  prep += tm.ms();
+
+  // keys + buckets
+  if (p.framework == 1) {
+    make_keys(I, X, n, &I.keys, err.ptr, s);
+    I.offsets.alloc((size_t)I.tables * I.tableSize, s);
+    I.buckets.alloc((size_t)I.tables * n, s);
+    DevBuf<int> cursors((size_t)I.tables * I.tableSize, s);
+    launch_lsh_build(I.keys.ptr, n, I.tables, I.tableSize, I.offsets.ptr, I.buckets.ptr, cursors.ptr, s);
+  }
+
+  // sketches (generateHashes(isHashKeys = false), lshFramework.cuh:391)
+  const bool want_sketch = (p.framework == 0) ? (impl >= 3 && impl <= 6) : (impl >= 3 && impl <= 6);
+  if (want_sketch) {
+    LSHG_REQUIRE(p.sketchDim >= 1, "sketchDim must be >= 1");
+    I.sk_kind = impl;
+    switch (impl) {
+      case 3: {
+        I.words = p.sketchDim;
+        LSHG_REQUIRE(I.words <= 64, "SimHash sketchDim must be <= 64 words");
+        I.wp = (I.words + 3) / 4 * 4;
+        std::vector<float> R((size_t)d * 32 * p.sketchDim);
+        random_normals((int64_t)R.size(), 1.0, R.data());  // simHash.cu:73 / lshFramework.cuh:24-27
+        upload(I.sk_planes, R.data(), R.size(), s);
+        break;
+      }
+      case 4:
+        I.sbytes = p.sketchDim;
+        I.words = (p.sketchDim + 3) / 4;
+        I.wp = (I.words + 3) / 4 * 4;
+        LSHG_REQUIRE(I.wp <= 64, "byte weighted-MinHash sketchDim must be <= 256");
+        wmh_prepare(I.wmh_sk, I.ops_sketch, X, n, comp, nc, d, p.sketchDim, 0, 0, 0, s);
+        break;
+      case 5:
+        I.words = p.sketchDim;
+        I.wp = (I.words + 3) / 4 * 4;
+        LSHG_REQUIRE(I.wp <= 64, "one-bit weighted-MinHash sketchDim must be <= 64 words");
+        wmh_prepare(I.wmh_sk, I.ops_sketch, X, n, comp, nc, d, p.sketchDim * 32, 1, p.sketchDim, 32, s);
+        break;
+      case 6: {
+        I.sdim = p.sketchDim;
+        if (p.framework == 1) do_normalize(I.ops_sketch, X, n, comp, nc, d, s);  // runGenericJL, simHashJL.cuh:254
+        std::vector<float> R((size_t)p.sketchDim * d);
+        random_normals((int64_t)R.size(), 1.0 / p.sketchDim, R.data());  // randomVectorGenerator.cpp:56-74
+        upload(I.sk_planes, R.data(), R.size(), s);
+        break;
+      }
+    }
+    DevBuf<uint32_t> packed;
+    DevBuf<float> fl;
+    make_sketch(I, X, n, 0x00, &packed, &fl, err.ptr, s);
+    if (impl == 6) {
+      I.xsf = std::move(fl);
+      I.xsft.alloc((size_t)ceil_div(n, 128) * 128 * I.sdim, s);
+      launch_tile_transpose(I.xsf.ptr, n, I.sdim, I.xsft.ptr, s);
+    } else {
+      I.xs = std::move(packed);
+    }
+  }
+
+  // exact-distance arrays
+  if (I.dist == DIST_ANGULAR) {
+    I.xnorm.alloc(n, s);
+    launch_row_norms(X, n, d, I.xnorm.ptr, s);
+  }
+  if (p.framework == 0 && impl == 2) {
+    I.xt.alloc((size_t)ceil_div(n, 128) * 128 * d, s);
+    launch_tile_transpose(X, n, d, I.xt.ptr, s);
+  }
+  if (p.framework == 0 && impl == 8) tc_prepare(I, s);
+  if (p.framework == 1) I.lsh_grid = lsh_query_grid(1 << 30);
+  check_err_flag(err.ptr, s);
+  build += tm.ms();
+  if (prep_ms) *prep_ms = prep;
+  if (build_ms) *build_ms = build;
+  return idx;
+}
+
+void sketch_queries(Index& I, float* q, int nq, DevBuf<uint32_t>* qs, DevBuf<float>* qsf, DevBuf<uint16_t>* qkeys,
+                    cudaStream_t s) {
+  apply_ops(I.ops_keys, q, nq, I.d, s);
+  if (I.p.framework == 1 && qkeys) make_keys(I, q, nq, qkeys, I.qerr.ptr, s);
+  apply_ops(I.ops_sketch, q, nq, I.d, s);
+  if (I.sk_kind) make_sketch(I, q, nq, 0xff, qs, qsf, I.qerr.ptr, s);
+}
+
+void query_error(Index& I, cudaStream_t s) {
+  int e = 0;
+  LSHG_CUDA(cudaMemcpyAsync(&e, I.qerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LSHG_CUDA(cudaStreamSynchronize(s));
+  if (e) {
+    LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
+    throw Error(LSHG_ERR_SAMPLER_LIMIT, "weighted MinHash sampler exceeded its draw limit (zero or NaN query?)");
+  }
+}
+
+void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
+  LSHG_REQUIRE(k >= 1 && k <= 4096, "k must be in [1, 4096]");
+  if (nq <= 0) return;
+  const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
+  DevBuf<uint32_t> qs;
+  DevBuf<float> qsf;
+  DevBuf<uint16_t> qkeys;
+  sketch_queries(I, q, nq, &qs, &qsf, &qkeys, s);
+  DevBuf<float> qnorm;
+  if (I.dist == DIST_ANGULAR) {
+    qnorm.alloc(nq, s);
+    launch_row_norms(q, nq, I.d, qnorm.ptr, s);
+  }
+  const int kp = std::max(32, next_pow2(k));
+  if (I.p.framework == 1) {
+    LshQueryArgs a{};
+    a.qkeys = qkeys.ptr;
+    a.nq = nq;
+    a.tables = I.tables;
+    a.tableSize = I.tableSize;
+    a.n = I.n;
+    a.offsets = I.offsets.ptr;
+    a.buckets = I.buckets.ptr;
+    a.x = I.x.ptr;
+    a.xnorm = I.xnorm.ptr;
+    a.q = q;
+    a.qnorm = qnorm.ptr;
+    a.d = I.d;
+    a.dist = I.dist;
+    a.sketched = (I.p.runWithSketchedData && I.sk_kind) ? 1 : 0;
+    a.sketch_kind = I.sk_kind;
+    a.xs = I.xs.ptr;
+    a.qs = qs.ptr;
+    a.wp = I.wp;
+    a.words = I.words;
+    a.sbytes = I.sbytes;
+    a.xsf = I.xsf.ptr;
+    a.qsf = qsf.ptr;
+    a.sdim = I.sdim;
+    a.C = a.sketched ? std::max(I.C, kp) : kp;
+    a.k = k;
+    a.grid = std::min(I.lsh_grid, lsh_query_grid(nq));
+    // per-call dedupe bitmaps: concurrent queries on one index never share them
+    DevBuf<uint32_t> bm((size_t)a.grid * ((I.n + 31) / 32), s);
+    LSHG_CUDA(cudaMemsetAsync(bm.ptr, 0, bm.bytes(), s));
+    a.bitmaps = bm.ptr;
+    launch_lsh_query(a, out, s);
+    return;
+  }
+  if (impl == 8) {
+    launch_tc_scan(I, q, nq, k, out, s);
+    return;
+  }
+  if (impl == 2) {
+    const int C = kp;
+    int splits = scan_float_splits(I.n, nq, C);
+    DevBuf<uint64_t> part((size_t)nq * splits * C, s);
+    launch_scan_float(I.xt.ptr, I.n, I.d, I.xnorm.ptr, q, nq, qnorm.ptr, I.dist, C, splits, part.ptr, s);
+    const uint64_t* keys = part.ptr;
+    DevBuf<uint64_t> merged;
+    if (splits > 1) {
+      merged.alloc((size_t)nq * C, s);
+      launch_merge_splits(part.ptr, nq, splits, C, merged.ptr, s);
+      keys = merged.ptr;
+    }
+    launch_keys_to_points(keys, nq, C, k, out, s);
+    return;
+  }
+  const int C = std::max(I.C, kp);
+  DevBuf<uint64_t> part;
+  int splits;
+  if (impl == 6) {
+    splits = scan_float_splits(I.n, nq, C);
+    part.alloc((size_t)nq * splits * C, s);
+    launch_scan_float(I.xsft.ptr, I.n, I.sdim, nullptr, qsf.ptr, nq, nullptr, DIST_SQEUCLID, C, splits, part.ptr, s);
+  } else {
+    splits = scan_bits_splits(I.n, nq, C);
+    part.alloc((size_t)nq * splits * C, s);
+    int op = impl == 3 ? OP_HAMMING : (impl == 4 ? OP_BYTE_JACCARD : OP_ONEBIT_JACCARD);
+    launch_scan_bits(I.xs.ptr, I.n, I.wp, I.words, I.sbytes, qs.ptr, nq, op, C, splits, part.ptr, s);
+  }
+  const uint64_t* cand = part.ptr;
+  DevBuf<uint64_t> merged;
+  if (splits > 1) {
+    merged.alloc((size_t)nq * C, s);
+    launch_merge_splits(part.ptr, nq, splits, C, merged.ptr, s);
+    cand = merged.ptr;
+  }
+  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s);
+}
+
+}  // namespace lshg

@@ -1,0 +1,114 @@
+// Resident index: the reference's pipelines (linearScans / runLsh) split into a build
+// step that leaves every derived array in HBM and a query step that only touches the
+// query batch.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace lshg {
+
+// In-place transformation applied to the base (and replayed on queries), in the order
+// the reference applies them to both arrays.
+struct PrepOp {
+  enum Kind { NORMALIZE = 0, SHIFT = 1 } kind;
+  std::vector<int> minv;                 // SHIFT: per-dimension min of floor (shift is |minv|)
+  std::shared_ptr<DevBuf<int>> dminv;    // device copy, so replay needs no host upload
+};
+
+// Weighted MinHash sampler state (weightedMinHash.cuh:345-468).
+struct WmhState {
+  bool used = false;
+  int M = 0;
+  int H = 0, T = 0;
+  int onebit = 0, words = 0, hashBits = 0;
+  DevBuf<int> start, map, seeds;
+  DevBuf<float> rtab;
+  DevBuf<unsigned char> states;
+  DevBuf<uint8_t> bitmap;
+  int bitmapLen = 255;
+  std::vector<int> h_start, h_map;  // kept for export / persistence
+};
+
+struct Index {
+  lshg_index_params p{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t n = 0;
+  int d = 0;
+
+  // base rows after preprocessing, magnitudes, and the 128-point tile layout
+  DevBuf<float> x, xnorm, xt;
+  int dist = DIST_ANGULAR;  // exact / re-rank distance
+  int C = 0;                // candidate count for sketched scans
+
+  std::vector<PrepOp> ops_keys;    // applied before keys are computed
+  std::vector<PrepOp> ops_sketch;  // applied after keys, before sketches
+
+  // sketches: kind 0 none, 3 SimHash, 4 byte WMH, 5 one-bit WMH, 6 JL
+  int sk_kind = 0;
+  int words = 0, wp = 0, sbytes = 0, sdim = 0;
+  DevBuf<uint32_t> xs;       // packed sketches, rows of wp words
+  DevBuf<float> xsf, xsft;   // JL sketches [n][sdim] and their tile layout
+  DevBuf<float> sk_planes;   // SimHash planes [32*sketchDim][d] or JL rows [sdim][d]
+  WmhState wmh_sk;
+
+  // LSH
+  int key_kind = 0;
+  int tableSize = 0, tables = 0, key_bits = 0;
+  DevBuf<uint16_t> keys;     // [n][tables]
+  DevBuf<int> offsets, buckets;
+  DevBuf<float> key_planes;  // SimHash key planes [tables*bits][d]
+  DevBuf<int> cp_diag;       // [tables][hashes][rounds][P]
+  int cp_P = 0, cp_hashes = 1, cp_rounds = 3;
+  WmhState wmh_keys;
+  DevBuf<uint32_t> bitmaps;  // per-CTA dedupe bitmaps of the LSH query
+  int lsh_grid = 0;
+
+  // tensor-core exact scan (implementation 8)
+  DevBuf<uint16_t> xbf;      // bf16 rows padded to dp
+  DevBuf<float> xbf_scale;   // unused for bf16 (kept for an fp8 layout)
+  int dp = 0;
+
+  // device error flag of the query path (weighted-MinHash draw limit); read by callers
+  // after the query has completed, so the query itself never synchronises
+  DevBuf<int> qerr;
+
+  ~Index();
+};
+
+// Build from a device copy of the base.  `companion` (optional, device, nq rows) are
+// queries the reference would transform alongside the base: preprocessing statistics
+// (Jaccard min shift, MinHash bounds) then cover base and companion, as in the
+// reference.  The companion buffer is transformed in place.
+std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& base, int64_t n, float* companion,
+                                   int ncomp, cudaStream_t stream, double* prep_ms, double* build_ms);
+
+// Answer nq device-resident queries (row-major, d floats) into device points.  The
+// query buffer is transformed in place.  Stream-ordered with no host synchronisation
+// and no pageable copies, so it can be recorded into a CUDA graph; callers check
+// query_error() after the stream has completed.
+void query_index(Index& idx, float* q, int nq, int k, lshg_point* out, cudaStream_t stream);
+// Throws if the last completed query raised the device error flag (clears it).
+void query_error(Index& idx, cudaStream_t stream);
+
+// Sketch / key a device query batch (after replaying the preprocessing).
+void sketch_queries(Index& idx, float* q, int nq, DevBuf<uint32_t>* qs, DevBuf<float>* qsf,
+                    DevBuf<uint16_t>* qkeys, cudaStream_t stream);
+
+int next_pow2(int v);
+
+// Persistence (persist.cpp): checksummed binary image of a built index.
+void save_index(const Index& idx, const char* path);
+std::unique_ptr<Index> load_index(const char* path, cudaStream_t stream);
+
+}  // namespace lshg
+
+// The C handle owns the index.
+struct lshg_index {
+  std::unique_ptr<lshg::Index> impl;
+};

@@ -1,0 +1,128 @@
+// Host-side launchers for every device kernel of the engine.  All pointers are device
+// pointers; every launcher is asynchronous on `stream`.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lshg {
+
+// Distance-function codes of the reference (distanceFunctions.cuh:54-71) plus the
+// squared Euclidean used on JL sketches (distanceFunctions.cuh:87-99).
+enum DistFunc : int { DIST_ANGULAR = 1, DIST_JACCARD = 2, DIST_EUCLID = 3, DIST_SQEUCLID = 4 };
+
+// Sketched-distance codes (runSketchedDistanceFunction, distanceFunctions.cuh:136-154).
+enum BitOp : int { OP_HAMMING = 3, OP_BYTE_JACCARD = 4, OP_ONEBIT_JACCARD = 5 };
+
+// ---- preprocess.cu ---------------------------------------------------------------
+// sqrt(sequential fmaf sum of squares) per row, exactly as the reference computes
+// magnitudes (distanceFunctions.cuh:31-36, processingUtils.cuh:55-60).
+void launch_row_norms(const float* x, int64_t n, int d, float* norms, cudaStream_t s);
+// In-place x /= norm (transformToUnitVectors, processingUtils.cuh:48-67).
+void launch_normalize(float* x, int64_t n, int d, cudaStream_t s);
+// Point-tile layout for the SIMT scans: xt[tile][j][128], zero padded.
+void launch_tile_transpose(const float* x, int64_t n, int d, float* xt, cudaStream_t s);
+// Jaccard shift (transformData, processingUtils.cuh:12-46): per-dim min of floor(x).
+void launch_min_floor(const float* x, int64_t n, int d, int* minv, cudaStream_t s);
+void launch_shift_abs(float* x, int64_t n, int d, const int* minv, cudaStream_t s);
+// WMH bounds (weightedMinHash.cuh:41-69): per-dim max of ceil(x).
+void launch_max_ceil(const float* x, int64_t n, int d, int* maxv, cudaStream_t s);
+// Fill helpers.
+void launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
+void launch_u32_to_u16(const uint32_t* in, int64_t n, uint16_t* out, cudaStream_t s);
+void launch_u32_to_u8(const uint32_t* in, int64_t n, uint8_t* out, cudaStream_t s);
+// Pad rows of `words` 32-bit words to `wp` words (pad value `pad`).
+void launch_pad_words(const uint32_t* in, int64_t n, int words, uint32_t* out, int wp, uint32_t pad,
+                      cudaStream_t s);
+
+// ---- project.cu ------------------------------------------------------------------
+// Projections with the reference's sequential FP32 FMA chain in dimension order.
+// mode 0: sign bits (simHash.cuh:20-46): plane p = w*bits + b sets bit b of word w.
+//         out32 must be zeroed when bits != 32.
+// mode 1: floats (JL, simHashJL.cuh:34-51): out_f[i*planes + p].
+void launch_project(const float* x, int64_t n, int d, const float* planes, int nplanes, int mode,
+                    int bits, int words, uint32_t* out32, float* out_f, cudaStream_t s);
+
+// ---- crosspoly.cu ----------------------------------------------------------------
+// Cross-polytope keys (crossPolyTope.cuh:25-85) with `hashes` concatenated hashes per
+// table (reference: 1).  diag: int[tables][hashes][rounds][P] of +-1.
+void launch_crosspoly(const float* x, int64_t n, int d, int P, int tables, int hashes, int rounds,
+                      const int* diag, uint16_t* keys, cudaStream_t s);
+
+// ---- wmh.cu ----------------------------------------------------------------------
+// Draw tables of the rejection sampler (weightedMinHash.cuh:109-166): for each seed,
+// curand_init(seed, 0, 10000) then T draws r = M * curand_uniform.  Layout r[j*H + h];
+// the XORWOW state after T draws is kept for continuation.
+void launch_wmh_tables(const int* seeds, int H, int T, int M, float* r, void* states, cudaStream_t s);
+// Samples: counter = number of red draws before the first green one.
+//  onebit = 0: out8[i*H + h] = counter mod 256 (sketchDataOriginal)
+//  onebit = 1: bit b of out32[i*words + w] = bitmap[counter] (sketchDataOneBit), with
+//              seed index h = w*hashBits + b.
+void launch_wmh_sketch(const float* x, int64_t n, int d, const int* start, const int* map, int M,
+                       const float* r, const void* states, int H, int T, int onebit, int words,
+                       int hashBits, const uint8_t* bitmap, int bitmapLen, uint8_t* out8,
+                       uint32_t* out32, int* err, cudaStream_t s);
+
+// ---- scan_float.cu ---------------------------------------------------------------
+// Top-C keys per (query, split) over float vectors (exact scans and JL sketches).
+// xt: tile layout of the base; q: row-major queries; norms only for DIST_ANGULAR.
+// out: [nq][splits][C] ascending keys.  Returns the number of splits used.
+int launch_scan_float(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq,
+                      const float* qnorm, int dist, int C, int splits, uint64_t* out, cudaStream_t s);
+int scan_float_splits(int64_t n, int nq, int C);
+
+// ---- scan_bits.cu ----------------------------------------------------------------
+// Top-C keys per (query, split) over packed sketches: rows of wp 32-bit words
+// (wp % 4 == 0) holding `words` real words (bytes for OP_BYTE_JACCARD: `sbytes` real).
+int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs,
+                     int nq, int op, int C, int splits, uint64_t* out, cudaStream_t s);
+int scan_bits_splits(int64_t n, int nq, int C);
+
+// ---- rerank.cu -------------------------------------------------------------------
+// Merge per-split sorted lists into one sorted list of C keys per query.
+void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
+// Exact re-rank of candidate keys (candidateSetScanner.cuh:10-32) and top-k output.
+void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d,
+                   const float* xnorm, const float* q, const float* qnorm, int dist, int k,
+                   struct ::lshg_point_s* out, cudaStream_t s);
+// Keys to result points (ID, distance); empty keys become (-1, INT_MAX).
+void launch_keys_to_points(const uint64_t* keys, int nq, int C, int k, struct ::lshg_point_s* out,
+                           cudaStream_t s);
+
+// ---- lsh.cu ----------------------------------------------------------------------
+// Bucket tables (lshFramework.cuh:102-140): counts -> absolute offsets -> ids.
+// keys: [n][tables] (u16 or u8 widened to u16).  offsets: [tables][tableSize],
+// buckets: [tables][n].
+void launch_lsh_build(const uint16_t* keys, int64_t n, int tables, int tableSize, int* offsets,
+                      int* buckets, int* cursors, cudaStream_t s);
+
+struct LshQueryArgs {
+  const uint16_t* qkeys;  // [nq][tables]
+  int nq, tables, tableSize;
+  int64_t n;
+  const int* offsets;
+  const int* buckets;
+  // exact data
+  const float* x;
+  const float* xnorm;
+  const float* q;
+  const float* qnorm;
+  int d;
+  int dist;  // rerank / exact distance function
+  // sketched data (optional)
+  int sketched;  // 0: exact distances on candidates; 1: sketch distance then rerank
+  int sketch_kind;  // 3 hamming, 4 byte, 5 onebit, 6 JL (float)
+  const uint32_t* xs;
+  const uint32_t* qs;
+  int wp, words, sbytes;
+  const float* xsf;  // JL sketches [n][sdim]
+  const float* qsf;
+  int sdim;
+  int C;  // candidate count kept before re-rank (sketched) or pow2 >= k (exact)
+  int k;
+  uint32_t* bitmaps;  // per-CTA dedupe bitmaps [grid][ceil(n/32)]
+  int grid;
+};
+void launch_lsh_query(const LshQueryArgs& a, struct ::lshg_point_s* out, cudaStream_t s);
+
+}  // namespace lshg

@@ -1,0 +1,135 @@
+// Split merge, exact re-rank of candidate sets and result write-out.
+//
+// The re-rank restates candidateSetScan (candidateSetScanner.cuh:10-32): every
+// candidate's exact distance is recomputed with the reference's arithmetic (one thread
+// walks one candidate row in dimension order), then the candidates are sorted by
+// (distance, id) and the first k written in ascending order -- the order the reference
+// produces by writing its sorted warp queue back to front (sketchedDistanceScanners.cuh:
+// 84-99).  Empty candidates (no point) become (-1, INT_MAX) as in the reference.
+#include "common.cuh"
+#include "kernels.h"
+#include "launch_count.h"
+#include "select.cuh"
+#include "distance.cuh"
+#include "profile.h"
+
+namespace lshg {
+
+namespace {
+
+// One block per query: fold S sorted lists of C keys into one.
+__global__ void merge_splits_kernel(const uint64_t* __restrict__ in, int nq, int splits, int C,
+                                    uint64_t* __restrict__ out) {
+  extern __shared__ uint64_t ms[];
+  const int q = blockIdx.x;
+  const uint64_t* src = in + (int64_t)q * splits * C;
+  for (int i = threadIdx.x; i < C; i += blockDim.x) ms[i] = src[i];
+  __syncthreads();
+  for (int s = 1; s < splits; ++s) {
+    const uint64_t* lst = src + (int64_t)s * C;
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+      uint64_t b = lst[C - 1 - i];
+      if (b < ms[i]) ms[i] = b;
+    }
+    __syncthreads();
+    block_bitonic_merge(ms, C);
+  }
+  for (int i = threadIdx.x; i < C; i += blockDim.x) out[(int64_t)q * C + i] = ms[i];
+}
+
+template <int DIST>
+__global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
+                              int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
+                              const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(rsm);
+  float* qr = reinterpret_cast<float*>(rsm + (size_t)C * 8);
+  const int qi = blockIdx.x;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) qr[j] = q[(int64_t)qi * d + j];
+  __syncthreads();
+  const float qn = (DIST == DIST_ANGULAR) ? qnorm[qi] : 1.0f;
+  for (int i = threadIdx.x; i < C; i += blockDim.x) {
+    uint64_t kin = cand[(int64_t)qi * C + i];
+    uint64_t ko = kEmptyKey;
+    if (kin != kEmptyKey) {
+      int id = key_id(kin);
+      if (id >= 0 && id < n) {
+        float xn = (DIST == DIST_ANGULAR) ? xnorm[id] : 1.0f;
+        ko = make_key(exact_distance<DIST>(x + (int64_t)id * d, qr, d, qn, xn), id);
+      }
+    }
+    keys[i] = ko;
+  }
+  __syncthreads();
+  block_bitonic_sort(keys, C);
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    uint64_t kk = i < C ? keys[i] : kEmptyKey;
+    lshg_point pt;
+    if (kk == kEmptyKey) { pt.ID = -1; pt.distance = kEmptyDistance; }
+    else { pt.ID = key_id(kk); pt.distance = key_dist(kk); }
+    out[(int64_t)qi * k + i] = pt;
+  }
+}
+
+__global__ void keys_to_points_kernel(const uint64_t* __restrict__ keys, int nq, int C, int k,
+                                      lshg_point* __restrict__ out) {
+  int64_t total = (int64_t)nq * k;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t qi = t / k;
+    int i = (int)(t - qi * k);
+    uint64_t kk = i < C ? keys[qi * C + i] : kEmptyKey;
+    lshg_point pt;
+    if (kk == kEmptyKey) { pt.ID = -1; pt.distance = kEmptyDistance; }
+    else { pt.ID = key_id(kk); pt.distance = key_dist(kk); }
+    out[t] = pt;
+  }
+}
+
+}  // namespace
+
+void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s) {
+  if (nq <= 0) return;
+  ProfScope _ps("merge_splits", s);
+  size_t smem = (size_t)C * 8;
+  LSHG_CUDA(cudaFuncSetAttribute(merge_splits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  merge_splits_kernel<<<nq, 128, smem, s>>>(in, nq, splits, C, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d, const float* xnorm,
+                   const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s) {
+  if (nq <= 0) return;
+  LSHG_REQUIRE((C & (C - 1)) == 0 && C >= 2, "re-rank: candidate count must be a power of two");
+  size_t smem = (size_t)C * 8 + (size_t)d * 4 + 16;
+  LSHG_REQUIRE(smem <= 200 * 1024, "re-rank: candidate set too large");
+  ProfScope _ps("rerank", s);
+  int threads = C >= 256 ? 256 : 128;
+#define LSHG_RR(DV)                                                                                       \
+  do {                                                                                                    \
+    LSHG_CUDA(cudaFuncSetAttribute(rerank_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+    rerank_kernel<DV><<<nq, threads, smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out);           \
+  } while (0)
+  switch (dist) {
+    case DIST_ANGULAR: LSHG_RR(DIST_ANGULAR); break;
+    case DIST_JACCARD: LSHG_RR(DIST_JACCARD); break;
+    case DIST_EUCLID: LSHG_RR(DIST_EUCLID); break;
+    case DIST_SQEUCLID: LSHG_RR(DIST_SQEUCLID); break;
+    default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "re-rank: invalid distance function");
+  }
+#undef LSHG_RR
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_keys_to_points(const uint64_t* keys, int nq, int C, int k, lshg_point* out, cudaStream_t s) {
+  if (nq <= 0) return;
+  ProfScope _ps("keys_to_points", s);
+  int64_t total = (int64_t)nq * k;
+  int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 8);
+  keys_to_points_kernel<<<blocks, 256, 0, s>>>(keys, nq, C, k, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+}  // namespace lshg

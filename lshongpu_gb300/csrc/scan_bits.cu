@@ -1,0 +1,193 @@
+// Sketched-distance linear scans over packed sketches with fused top-C selection.
+//
+// Replaces scanHammingDistance (sketchedDistanceScanners.cuh:14-100) and
+// scanJaccardDistance (:194-274).  Distances are the reference's, as floats:
+//   Hamming        sum popc(q ^ x)                                 (distanceFunctions.cuh:73-85)
+//   one-bit WMH    1 - sum(32 - popc(q ^ x)) / (32 * words)         (:118-134)
+//   byte WMH       1 - (#equal bytes) / sketchDim                   (:102-116)
+// GB300 form: a CTA owns QB queries (sketches in shared memory) and a split of the
+// base; each thread holds one point's sketch in registers (loaded with 128-bit,
+// coalesced loads) and scores it against its half of the CTA's queries with XOR and
+// popcount.  Candidates are filtered against each query's running threshold and
+// folded into a per-query sorted top-C list (select.cuh).
+#include "common.cuh"
+#include "kernels.h"
+#include "launch_count.h"
+#include "profile.h"
+#include "select.cuh"
+
+namespace lshg {
+
+namespace {
+
+constexpr int kTile = 128;      // points per tile (one per thread of each half)
+constexpr int kBuf = 256;
+constexpr int kMaxChunks = 16;  // up to 64 words (2048 bits) per sketch
+
+struct BitsSmem {
+  size_t qs, kept, buf, thr, cnt, total;
+};
+
+__host__ __device__ inline size_t smem_take(size_t& off, size_t bytes) {
+  off = (off + 15) / 16 * 16;
+  size_t at = off;
+  off += bytes;
+  return at;
+}
+
+__host__ __device__ inline BitsSmem bits_layout(int wp, int QB, int C) {
+  BitsSmem L;
+  size_t off = 0;
+  L.qs = smem_take(off, (size_t)QB * wp * 4);
+  L.kept = smem_take(off, (size_t)QB * C * 8);
+  L.buf = smem_take(off, (size_t)QB * kBuf * 8);
+  L.thr = smem_take(off, (size_t)QB * 8);
+  L.cnt = smem_take(off, (size_t)QB * 4);
+  L.total = off;
+  return L;
+}
+
+__device__ __forceinline__ int zero_bytes(uint32_t z) {
+  uint32_t t = (z & 0x7f7f7f7fu) + 0x7f7f7f7fu;
+  t = ~(t | z | 0x7f7f7f7fu);
+  return __popc(t);
+}
+
+template <int OP>
+__device__ __forceinline__ int word_score(uint32_t a, uint32_t b) {
+  if (OP == OP_BYTE_JACCARD) return zero_bytes(a ^ b);
+  return __popc(a ^ b);
+}
+
+template <int OP, int QB>
+__global__ void __launch_bounds__(256) scan_bits_kernel(const uint32_t* __restrict__ xs, int64_t n, int wp, int words,
+                                                        int sbytes, const uint32_t* __restrict__ qs, int nq, int C,
+                                                        int tiles_per_split, int splits, uint64_t* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const BitsSmem L = bits_layout(wp, QB, C);
+  uint32_t* qsm = reinterpret_cast<uint32_t*>(smem + L.qs);
+  TopCShared S{reinterpret_cast<uint64_t*>(smem + L.kept), reinterpret_cast<uint64_t*>(smem + L.buf),
+               reinterpret_cast<int*>(smem + L.cnt), reinterpret_cast<uint64_t*>(smem + L.thr), C, kBuf};
+
+  const int q0 = blockIdx.x * QB;
+  const int split = blockIdx.y;
+  const int ntiles = (int)((n + kTile - 1) / kTile);
+  const int t_begin = split * tiles_per_split;
+  const int t_end = min(ntiles, t_begin + tiles_per_split);
+  const int nc = wp >> 2;
+
+  for (int i = threadIdx.x; i < QB * wp; i += blockDim.x) {
+    int qi = i / wp;
+    qsm[i] = (q0 + qi < nq) ? qs[(int64_t)(q0 + qi) * wp + (i - qi * wp)] : 0u;
+  }
+  topc_init(S, QB);
+  __syncthreads();
+
+  const int half = threadIdx.x >> 7;   // queries half, half+2, ...
+  const int pl = threadIdx.x & 127;    // point within the tile
+  constexpr int QPT = (QB + 1) / 2;    // queries per thread
+  uint64_t thr[QPT];
+#pragma unroll
+  for (int a = 0; a < QPT; ++a) thr[a] = kEmptyKey;
+
+  const float inv_div_f = (OP == OP_ONEBIT_JACCARD) ? (float)(32 * words) : (float)sbytes;
+
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    const int64_t p = (int64_t)tile * kTile + pl;
+    const bool valid = p < n;
+    uint4 xr[kMaxChunks];
+    const uint4* row = reinterpret_cast<const uint4*>(xs + (valid ? p : 0) * wp);
+#pragma unroll
+    for (int c = 0; c < kMaxChunks; ++c) xr[c] = (c < nc && valid) ? __ldg(&row[c]) : make_uint4(0, 0, 0, 0);
+
+    if (valid) {
+#pragma unroll
+      for (int a = 0; a < QPT; ++a) {
+        const int qi = half + 2 * a;
+        if (qi >= QB || q0 + qi >= nq) continue;
+        const uint4* qv = reinterpret_cast<const uint4*>(qsm + qi * wp);
+        int acc = 0;
+#pragma unroll
+        for (int c = 0; c < kMaxChunks; ++c) {
+          if (c < nc) {
+            uint4 b = qv[c];
+            acc += word_score<OP>(xr[c].x, b.x) + word_score<OP>(xr[c].y, b.y) + word_score<OP>(xr[c].z, b.z) +
+                   word_score<OP>(xr[c].w, b.w);
+          }
+        }
+        float dist;
+        if (OP == OP_HAMMING) {
+          dist = (float)acc;
+        } else if (OP == OP_ONEBIT_JACCARD) {
+          dist = __fsub_rn(1.0f, __fdiv_rn((float)(32 * words - acc), inv_div_f));
+        } else {
+          dist = __fsub_rn(1.0f, __fdiv_rn((float)acc, inv_div_f));
+        }
+        topc_push(S, qi, make_key(dist, (int)p), thr[a]);
+      }
+    }
+    topc_flush(S, QB, kBuf - kTile);
+#pragma unroll
+    for (int a = 0; a < QPT; ++a) {
+      const int qi = half + 2 * a;
+      if (qi < QB) thr[a] = S.thr[qi];
+    }
+  }
+  topc_flush(S, QB, 0);
+
+  for (int i = threadIdx.x; i < QB * C; i += blockDim.x) {
+    int qi = i / C, c = i - qi * C;
+    if (q0 + qi < nq) out[((int64_t)(q0 + qi) * splits + split) * C + c] = S.kept[(size_t)qi * C + c];
+  }
+}
+
+template <int OP, int QB>
+void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
+                int splits, uint64_t* out, cudaStream_t s) {
+  ProfScope _ps("scan_bits", s);
+  size_t smem = bits_layout(wp, QB, C).total;
+  auto kern = scan_bits_kernel<OP, QB>;
+  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int ntiles = ceil_div(n, kTile);
+  int tps = ceil_div(ntiles, splits);
+  dim3 grid(ceil_div(nq, QB), splits);
+  kern<<<grid, 256, smem, s>>>(xs, n, wp, words, sbytes, qs, nq, C, tps, splits, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+template <int OP>
+void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
+               int splits, uint64_t* out, cudaStream_t s) {
+  if (C <= 128) launch_cfg<OP, 32>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else if (C <= 1024) launch_cfg<OP, 8>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else launch_cfg<OP, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+}
+
+}  // namespace
+
+int scan_bits_splits(int64_t n, int nq, int C) {
+  int QB = C <= 128 ? 32 : (C <= 1024 ? 8 : 2);
+  int qblocks = ceil_div(nq, QB);
+  int ntiles = ceil_div(n, kTile);
+  int want = ceil_div((int64_t)num_sms() * 3, qblocks);
+  int maxs = std::max(1, ntiles / 4);
+  return std::max(1, std::min(std::min(want, maxs), 64));
+}
+
+int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int op,
+                     int C, int splits, uint64_t* out, cudaStream_t s) {
+  if (nq <= 0) return splits;
+  LSHG_REQUIRE(n > 0, "sketch scan: empty base");
+  LSHG_REQUIRE(wp % 4 == 0 && wp / 4 <= kMaxChunks, "sketch scan: rows must be 4..64 words, multiple of 4");
+  LSHG_REQUIRE(C >= 32 && C <= 4096 && (C & (C - 1)) == 0, "sketch scan: C must be a power of two in [32, 4096]");
+  switch (op) {
+    case OP_HAMMING: launch_op<OP_HAMMING>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    case OP_BYTE_JACCARD: launch_op<OP_BYTE_JACCARD>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    case OP_ONEBIT_JACCARD: launch_op<OP_ONEBIT_JACCARD>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "sketch scan: invalid sketch type");
+  }
+  return splits;
+}
+
+}  // namespace lshg

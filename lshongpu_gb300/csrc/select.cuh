@@ -1,0 +1,158 @@
+// Top-C selection primitives on 64-bit ordering keys (see common.cuh).
+//
+// This replaces the reference's per-lane thread queues + lane-stride bitonic sort
+// (LinearScan/sortingFramework.cuh:163-254) and its buffered insert rule
+// (sketchedDistanceScanners.cuh:68-80).  Design:
+//   * each query owns, in shared memory, a sorted "kept" list of its C best keys and an
+//     unsorted append buffer;
+//   * producers push a key only if it beats the query's current threshold (the C-th
+//     kept key, a monotonically tightening upper bound), appending with a shared-memory
+//     atomic;
+//   * when a buffer might overflow, one warp sorts it (bitonic, in shared memory) and
+//     folds it into the kept list with a single bitonic "min + merge" pass.
+// All orderings are on (distance, id) so results do not depend on thread timing.
+#pragma once
+
+#include "common.cuh"
+
+namespace lshg {
+
+__device__ __forceinline__ int next_pow2_dev(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+// Warp-cooperative ascending bitonic sort of n (power of two) keys in shared memory.
+__device__ __forceinline__ void warp_bitonic_sort(uint64_t* a, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int size = 2; size <= n; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = lane; t < (n >> 1); t += 32) {
+        int i = 2 * t - (t & (stride - 1));
+        int j = i + stride;
+        bool up = ((i & size) == 0);
+        uint64_t x = a[i], y = a[j];
+        if ((x > y) == up) { a[i] = y; a[j] = x; }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Warp-cooperative ascending sort of a bitonic sequence of n (power of two) keys.
+__device__ __forceinline__ void warp_bitonic_merge(uint64_t* a, int n) {
+  const int lane = threadIdx.x & 31;
+  for (int stride = n >> 1; stride > 0; stride >>= 1) {
+    for (int t = lane; t < (n >> 1); t += 32) {
+      int i = 2 * t - (t & (stride - 1));
+      int j = i + stride;
+      uint64_t x = a[i], y = a[j];
+      if (x > y) { a[i] = y; a[j] = x; }
+    }
+    __syncwarp();
+  }
+}
+
+// Block-cooperative ascending bitonic sort of n (power of two) keys in shared memory.
+// Every thread of the block must call it.
+__device__ __forceinline__ void block_bitonic_sort(uint64_t* a, int n) {
+  for (int size = 2; size <= n; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
+        int i = 2 * t - (t & (stride - 1));
+        int j = i + stride;
+        bool up = ((i & size) == 0);
+        uint64_t x = a[i], y = a[j];
+        if ((x > y) == up) { a[i] = y; a[j] = x; }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Block-cooperative ascending sort of a bitonic sequence of n (power of two) keys.
+__device__ __forceinline__ void block_bitonic_merge(uint64_t* a, int n) {
+  for (int stride = n >> 1; stride > 0; stride >>= 1) {
+    for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
+      int i = 2 * t - (t & (stride - 1));
+      int j = i + stride;
+      uint64_t x = a[i], y = a[j];
+      if (x > y) { a[i] = y; a[j] = x; }
+    }
+    __syncthreads();
+  }
+}
+
+// Fold an unsorted buffer of `cnt` keys into the sorted kept list of C keys (C a power
+// of two); afterwards kept holds the C smallest keys of the union, ascending.  `buf`
+// must have room for next_pow2(cnt) entries.  Executed by one full warp.
+__device__ __forceinline__ void warp_fold_buffer(uint64_t* kept, int C, uint64_t* buf, int cnt) {
+  const int lane = threadIdx.x & 31;
+  if (cnt <= 0) return;
+  int nb = next_pow2_dev(cnt < 2 ? 2 : cnt);
+  for (int i = cnt + lane; i < nb; i += 32) buf[i] = kEmptyKey;
+  __syncwarp();
+  warp_bitonic_sort(buf, nb);
+  // kept ascending, buffer ascending: min(kept[i], buf[C-1-i]) is bitonic and holds the
+  // C smallest keys of the union.
+  for (int i = lane; i < C; i += 32) {
+    int j = C - 1 - i;
+    uint64_t b = (j < nb) ? buf[j] : kEmptyKey;
+    if (b < kept[i]) kept[i] = b;
+  }
+  __syncwarp();
+  warp_bitonic_merge(kept, C);
+}
+
+// Per-query selection state in shared memory, laid out by the kernel:
+//   kept[q*C .. q*C+C)   sorted ascending
+//   buf [q*B .. q*B+B)   append buffer
+//   cnt[q], thr[q]
+struct TopCShared {
+  uint64_t* kept;
+  uint64_t* buf;
+  int* cnt;
+  uint64_t* thr;
+  int C;
+  int B;
+};
+
+__device__ __forceinline__ void topc_init(TopCShared s, int nq) {
+  for (int i = threadIdx.x; i < nq * s.C; i += blockDim.x) s.kept[i] = kEmptyKey;
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    s.cnt[q] = 0;
+    s.thr[q] = kEmptyKey;
+  }
+}
+
+// Append `key` for query q if it beats the threshold snapshot `thr`.
+__device__ __forceinline__ void topc_push(TopCShared s, int q, uint64_t key, uint64_t thr) {
+  if (key < thr) {
+    int p = atomicAdd(&s.cnt[q], 1);
+    s.buf[(size_t)q * s.B + p] = key;
+  }
+}
+
+// Merge the buffers of every query whose fill exceeds `limit` (or all non-empty buffers
+// when limit < 0).  Block-wide: all threads call it; warps take queries round-robin.
+// Returns after a __syncthreads so new thresholds are visible.
+__device__ __forceinline__ void topc_flush(TopCShared s, int nq, int limit) {
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  for (int q = warp; q < nq; q += nwarps) {
+    int c = s.cnt[q];
+    if (c > limit && c > 0) {
+      warp_fold_buffer(s.kept + (size_t)q * s.C, s.C, s.buf + (size_t)q * s.B, c);
+      if ((threadIdx.x & 31) == 0) {
+        s.cnt[q] = 0;
+        s.thr[q] = s.kept[(size_t)q * s.C + s.C - 1];
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace lshg

@@ -1,0 +1,206 @@
+"""ctypes binding of the CPU oracle (oracle.c, gold_port.cpp) -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module,
+as the checker.  The engine (lshongpu_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+P = C.c_void_p
+i64 = C.c_int64
+i32 = C.c_int
+
+_SIGS = {
+    "or_random_normals": (None, [i64, C.c_double, P]),
+    "or_random_plus_minus": (None, [i64, P]),
+    "or_random_bools": (None, [i64, P]),
+    "or_normalize": (None, [P, i64, i32]),
+    "or_row_norms": (None, [P, i64, i32, P]),
+    "or_jaccard_shift": (None, [P, i64, P, i64, i32]),
+    "or_exact_topk": (None, [P, i64, P, i64, i32, i32, i32, P, P]),
+    "or_fp64_topk": (None, [P, i64, P, i64, i32, i32, P, P]),
+    "or_fp64_topk_mt": (None, [P, i64, P, i64, i32, i32, i32, P, P]),
+    "or_simhash": (None, [P, i64, i32, P, i32, i32, P]),
+    "or_jl": (None, [P, i64, i32, P, i32, P]),
+    "or_crosspoly": (None, [P, i64, i32, i32, i32, i32, i32, P, P]),
+    "or_wmh_bounds": (i32, [P, i64, P, i64, i32, P, P, i32]),
+    "or_wmh_sketch": (i64, [P, i64, i32, P, P, i32, P, i32, i32, i32, i32, i32, P, i32, P, P]),
+    "or_sketch_scan": (None, [P, i64, P, i64, i32, i32, P, P, i32, i32, i32, i32, P, P, P]),
+    "or_lsh_build": (None, [P, i64, i32, i32, P, P]),
+    "or_lsh_query": (None, [P, i64, P, i64, i32, P, i32, i32, P, P, i32, i32, P, P, i32, i32, i32, i32, P, P]),
+    "or_goldstandard": (C.c_double, [P, i64, P, i64, i32, i32, i32, P, P]),
+}
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = _build.lib_path()
+        if not os.path.exists(path):
+            _build.build_oracle()
+        L = C.CDLL(path)
+        for n, (r, a) in _SIGS.items():
+            f = getattr(L, n)
+            f.restype, f.argtypes = r, a
+        _LIB = L
+    return _LIB
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def random_normals(count, stddev=1.0):
+    out = np.empty(count, np.float32)
+    lib().or_random_normals(count, stddev, _p(out))
+    return out
+
+
+def random_plus_minus(count):
+    out = np.empty(count, np.int32)
+    lib().or_random_plus_minus(count, _p(out))
+    return out
+
+
+def random_bools(count):
+    out = np.empty(count, np.uint8)
+    lib().or_random_bools(count, _p(out))
+    return out
+
+
+def normalize(x):
+    x = _f32(x).copy()
+    lib().or_normalize(_p(x), x.shape[0], x.shape[1])
+    return x
+
+
+def row_norms(x):
+    x = _f32(x)
+    out = np.empty(x.shape[0], np.float32)
+    lib().or_row_norms(_p(x), x.shape[0], x.shape[1], _p(out))
+    return out
+
+
+def jaccard_shift(x, q):
+    x, q = _f32(x).copy(), _f32(q).copy()
+    lib().or_jaccard_shift(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1])
+    return x, q
+
+
+def exact_topk(x, q, k, dist=1):
+    x, q = _f32(x), _f32(q)
+    ids = np.empty((q.shape[0], k), np.int32)
+    ds = np.empty((q.shape[0], k), np.float32)
+    lib().or_exact_topk(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1], dist, k, _p(ids), _p(ds))
+    return ids, ds
+
+
+def fp64_topk(x, q, k, threads=1):
+    x, q = _f32(x), _f32(q)
+    ids = np.empty((q.shape[0], k), np.int32)
+    ds = np.empty((q.shape[0], k), np.float64)
+    if threads > 1:
+        lib().or_fp64_topk_mt(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1], k, threads, _p(ids), _p(ds))
+    else:
+        lib().or_fp64_topk(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1], k, _p(ids), _p(ds))
+    return ids, ds
+
+
+def simhash(x, planes, words, bits):
+    x, planes = _f32(x), _f32(planes)
+    out = np.empty((x.shape[0], words), np.uint32)
+    lib().or_simhash(_p(x), x.shape[0], x.shape[1], _p(planes), words, bits, _p(out))
+    return out
+
+
+def jl(x, R, sdim):
+    x, R = _f32(x), _f32(R)
+    out = np.empty((x.shape[0], sdim), np.float32)
+    lib().or_jl(_p(x), x.shape[0], x.shape[1], _p(R), sdim, _p(out))
+    return out
+
+
+def crosspoly(x, P_, tables, hashes, rounds, diag):
+    x = _f32(x)
+    diag = np.ascontiguousarray(diag, np.int32)
+    out = np.empty((x.shape[0], tables), np.uint16)
+    lib().or_crosspoly(_p(x), x.shape[0], x.shape[1], P_, tables, hashes, rounds, _p(diag), _p(out))
+    return out
+
+
+def wmh_bounds(x, q):
+    x, q = _f32(x), _f32(q)
+    d = x.shape[1]
+    start = np.empty(d, np.int32)
+    cap = 1 << 20
+    mp = np.empty(cap, np.int32)
+    M = lib().or_wmh_bounds(_p(x), x.shape[0], _p(q), q.shape[0], d, _p(start), _p(mp), cap)
+    return start, mp[:M].copy(), M
+
+
+def wmh_sketch(x, start, mp, M, u, H, T, onebit, words, hashBits, bitmap):
+    """u: (H, T) float32 uniforms.  Returns (sketch, n_over_T)."""
+    x = _f32(x)
+    u = _f32(u)
+    bitmap = np.ascontiguousarray(bitmap, np.uint8)
+    n = x.shape[0]
+    out8 = np.zeros((n, H), np.uint8)
+    out32 = np.zeros((n, max(words, 1)), np.uint32)
+    over = lib().or_wmh_sketch(_p(x), n, x.shape[1], _p(np.ascontiguousarray(start, np.int32)),
+                               _p(np.ascontiguousarray(mp, np.int32)), M, _p(u), H, T, int(onebit), words, hashBits,
+                               _p(bitmap), len(bitmap), _p(out8), _p(out32))
+    return (out32 if onebit else out8), int(over)
+
+
+def sketch_scan(x, q, kind, xs, qs, width, C_, dist, k, want_cand=False):
+    x, q = _f32(x), _f32(q)
+    nq = q.shape[0]
+    ids = np.empty((nq, k), np.int32)
+    ds = np.empty((nq, k), np.float32)
+    cand = np.empty((nq, C_), np.uint64) if want_cand else None
+    xs, qs = np.ascontiguousarray(xs), np.ascontiguousarray(qs)
+    lib().or_sketch_scan(_p(x), x.shape[0], _p(q), nq, x.shape[1], kind, _p(xs), _p(qs), width, C_, dist, k,
+                         _p(cand), _p(ids), _p(ds))
+    return (ids, ds, cand) if want_cand else (ids, ds)
+
+
+def lsh_build(keys, tables, S):
+    keys = np.ascontiguousarray(keys, np.uint16)
+    n = keys.shape[0]
+    off = np.empty(tables * S, np.int32)
+    b = np.empty(tables * n, np.int32)
+    lib().or_lsh_build(_p(keys), n, tables, S, _p(off), _p(b))
+    return off, b
+
+
+def lsh_query(x, q, qkeys, tables, S, off, buckets, sketched, kind, xs, qs, width, C_, dist, k):
+    x, q = _f32(x), _f32(q)
+    nq = q.shape[0]
+    ids = np.empty((nq, k), np.int32)
+    ds = np.empty((nq, k), np.float32)
+    qkeys = np.ascontiguousarray(qkeys, np.uint16)
+    xs = None if xs is None else np.ascontiguousarray(xs)
+    qs = None if qs is None else np.ascontiguousarray(qs)
+    lib().or_lsh_query(_p(x), x.shape[0], _p(q), nq, x.shape[1], _p(qkeys), tables, S, _p(off), _p(buckets),
+                       int(sketched), kind, _p(xs), _p(qs), width, C_, dist, k, _p(ids), _p(ds))
+    return ids, ds
+
+
+def goldstandard(x, q, k, threads=1):
+    """Port of GoldStandard computeGoldStandard: returns (ids, -cos, seconds)."""
+    x, q = _f32(x), _f32(q)
+    ids = np.empty((q.shape[0], k), np.int32)
+    ds = np.empty((q.shape[0], k), np.float32)
+    t = lib().or_goldstandard(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1], k, threads, _p(ids), _p(ds))
+    return ids, ds, t

@@ -1,0 +1,84 @@
+"""GPU parity of the (K,L) LSH framework (lshFramework.cuh) against the CPU oracle:
+keys bit-exact, bucket tables identical (ids sorted within buckets), query results
+bit-exact (distinct candidates, top-k by (distance, id))."""
+import numpy as np
+import pytest
+
+from lshongpu_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+
+D = 100
+
+
+def data(n, nq, seed=21):
+    return datasets.clustered(n, D, seed, count=12), datasets.clustered(nq, D, seed + 1, count=12)
+
+
+def lsh_index_arrays(engine, idx, n, tables, S):
+    keys = np.frombuffer(idx.export(engine.EXPORT_KEYS), np.uint16).reshape(n, tables)
+    off = np.frombuffer(idx.export(engine.EXPORT_OFFSETS), np.int32)
+    bk = np.frombuffer(idx.export(engine.EXPORT_BUCKETS), np.int32)
+    return keys, off, bk
+
+
+@pytest.mark.parametrize("hashes,bits", [(1, 8), (2, 16)])
+def test_crosspoly_keys_buckets_query(engine, orc, hashes, bits):
+    n, nq, L, P = 4000, 16, 8, 128
+    x, q = data(n, nq)
+    S = 1 << bits
+    opt = engine.make_options(cp_hashes=hashes)
+    idx = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=bits,
+                       tables=L, options=opt)
+    xn, qn = orc.normalize(x), orc.normalize(q)
+    diag = engine.random_plus_minus(P * L * 3 * hashes)
+    okeys = orc.crosspoly(xn, P, L, hashes, 3, diag)
+    keys, off, bk = lsh_index_arrays(engine, idx, n, L, S)
+    assert np.array_equal(keys, okeys)
+    ooff, obk = orc.lsh_build(okeys, L, S)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(bk, obk)
+    _, qk = idx.sketch_queries(q, np.uint32, 0, L)
+    oqk = orc.crosspoly(qn, P, L, hashes, 3, diag)
+    assert np.array_equal(qk, oqk)
+    res = idx.query(q, 32)
+    ids, ds = orc.lsh_query(xn, qn, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, 1, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
+
+
+def test_simhash_keys_sketched_query(engine, orc):
+    n, nq, L, bits, W = 3000, 12, 6, 10, 8
+    x, q = data(n, nq, seed=31)
+    r = engine.LSH(3, 3, 32, D, nq, n, x, q, W, 1, bits, L, True, options=engine.make_options(candidates=512))
+    kp = engine.random_normals(L * D * bits)
+    okeys = (orc.simhash(x, kp, L, bits) & 0xFFFF).astype(np.uint16)
+    oqk = (orc.simhash(q, kp, L, bits) & 0xFFFF).astype(np.uint16)
+    S = 1 << bits
+    ooff, obk = orc.lsh_build(okeys, L, S)
+    sp = engine.random_normals(W * D * 32)
+    xs, qs = orc.simhash(x, sp, W, 32), orc.simhash(q, sp, W, 32)
+    ids, ds = orc.lsh_query(x, q, oqk, L, S, ooff, obk, 1, 3, xs, qs, W, 512, 1, 32)
+    assert np.array_equal(r.ids, ids)
+    assert np.array_equal(r.distances, ds)
+
+
+def test_lsh_exact_reference_entry_point(engine, orc):
+    n, nq, L, bits = 2500, 10, 4, 12
+    x, q = data(n, nq, seed=41)
+    r = engine.LSH(2, 3, 64, D, nq, n, x, q, 0, 1, bits, L, False)
+    kp = engine.random_normals(L * D * bits)
+    okeys = (orc.simhash(x, kp, L, bits) & 0xFFFF).astype(np.uint16)
+    oqk = (orc.simhash(q, kp, L, bits) & 0xFFFF).astype(np.uint16)
+    ooff, obk = orc.lsh_build(okeys, L, 1 << bits)
+    ids, ds = orc.lsh_query(x, q, oqk, L, 1 << bits, ooff, obk, 0, 0, None, None, 0, 64, 1, 64)
+    assert np.array_equal(r.ids, ids)
+    assert np.array_equal(r.distances, ds)
+    # fewer than k distinct candidates leave empty entries
+    assert ((r.ids == -1) == (ids == -1)).all()
+
+
+def test_lsh_bad_key_range_rejected(engine):
+    x, q = data(100, 2)
+    with pytest.raises(engine.LshgError):
+        engine.LSH(2, 7, 32, D, 2, 100, x, q, 0, 1, 6, 4, False)  # 2P = 256 keys > 2^6 buckets

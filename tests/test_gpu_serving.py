@@ -1,0 +1,81 @@
+"""Serving loop and persistence on the GPU: every request's result is the same alone
+and in the mix (continuous batching across streams, CUDA-graph replays), admission
+refuses what cannot fit, and a saved index answers like the original."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from lshongpu_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+
+D = 100
+
+
+@pytest.fixture(scope="module")
+def indexes(engine):
+    x = datasets.clustered(20000, D, 51, count=50)
+    exact = engine.Index(x, implementation=2, distanceFunc=1)
+    sim = engine.Index(x, implementation=3, sketchDim=16, options=engine.make_options(candidates=256))
+    cp = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=16,
+                      tables=8, options=engine.make_options(cp_hashes=2))
+    return x, {0: exact, 1: sim, 2: cp}
+
+
+def test_same_alone_and_in_the_mix(engine, indexes):
+    x, idx = indexes
+    rng = np.random.default_rng(3)
+    srv = engine.Server(max_batch=1024, streams=2, use_graphs=True)
+    for i, ix in idx.items():
+        srv.add_index(i, ix)
+    reqs = []
+    for t in range(60):
+        which = int(rng.integers(0, 3))
+        nq = int(np.exp(rng.uniform(0, np.log(300))))
+        k = int(rng.choice([10, 32, 100]))
+        q = datasets.clustered(nq, D, 1000 + t, count=50)
+        reqs.append((which, q, k, srv.submit(which, q, k)))
+    lat = []
+    for which, q, k, tk in reqs:
+        out, l = srv.wait(tk)
+        alone = idx[which].query(q, k)
+        assert np.array_equal(out, alone), f"request on index {which} differs in the mix"
+        lat.append(l)
+    st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["launches"] <= len(reqs)
+    assert st["graph_replays"] >= 1
+    assert min(lat) > 0
+    srv.close()
+
+
+def test_admission_by_free_hbm(engine, indexes):
+    _, idx = indexes
+    srv = engine.Server(hbm_reserve_mb=1 << 30)  # more than any GPU has: everything refused
+    srv.add_index(0, idx[0])
+    q = datasets.clustered(4, D, 9, count=50)
+    with pytest.raises(engine.LshgError) as e:
+        srv.submit(0, q, 32)
+    assert e.value.status == 7
+    assert srv.stats()["rejected"] == 1
+    srv.close()
+
+
+def test_persistence_roundtrip(engine, indexes):
+    x, idx = indexes
+    q = datasets.clustered(40, D, 77, count=50)
+    with tempfile.TemporaryDirectory() as td:
+        for i, ix in idx.items():
+            p = os.path.join(td, f"ix{i}.lshg")
+            ix.save(p)
+            re = engine.Index.load(p)
+            assert np.array_equal(re.query(q, 32), ix.query(q, 32))
+            with open(p, "r+b") as f:  # corrupt one byte: the checksum catches it
+                f.seek(100)
+                b = f.read(1)
+                f.seek(100)
+                f.write(bytes([b[0] ^ 0xFF]))
+            with pytest.raises(engine.LshgError):
+                engine.Index.load(p)
