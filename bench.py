@@ -159,8 +159,11 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--path", default="tc", choices=["tc", "exact", "simhash"])
     ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
+    ap.add_argument("--n", type=int, default=N_BASE, help="base size (profiling cases only)")
+    ap.add_argument("--nq", type=int, default=N_QUERY, help="queries per step (profiling cases only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    globals().update(N_BASE=args.n, N_QUERY=args.nq)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

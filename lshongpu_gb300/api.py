@@ -61,8 +61,7 @@ def profile_enable(on: bool = True) -> None:
 
 def profile_report() -> dict[str, tuple[int, float]]:
     """{kernel: (launches, total_ms)} since the last report (CUDA events on the launching stream)."""
-    need = lib().lshg_profile_report(None, 0)
-    buf = C.create_string_buffer(max(need, 1) + 4096)
+    buf = C.create_string_buffer(1 << 16)  # one call: reporting drains the records
     lib().lshg_profile_report(buf, len(buf))
     out = {}
     for line in buf.value.decode().splitlines():

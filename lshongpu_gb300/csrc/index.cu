@@ -440,6 +440,7 @@ void query_error(Index& I, cudaStream_t s) {
   LSHG_CUDA(cudaStreamSynchronize(s));
   if (e) {
     LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
+    if (e == 2) throw Error(LSHG_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out (kernel aborted)");
     throw Error(LSHG_ERR_SAMPLER_LIMIT, "weighted MinHash sampler exceeded its draw limit (zero or NaN query?)");
   }
 }

@@ -1,17 +1,454 @@
-// Tensor-core exact scan (implementation 8): placeholder until the tcgen05 kernel lands.
+// Tensor-core exact scan (implementation 8; no reference counterpart -- it replaces the
+// reference's FP32 exact scan, memOptimizedLinearScan.cu:20-106, for angular k-NN).
+//
+// Pipeline per query batch:
+//   1. queries -> unit rows in BF16, zero-padded to 128 dims (the base was converted the
+//      same way at build: x / |x|);
+//   2. tc_scan_kernel: BF16 GEMM Q x N on the 5th-generation tensor cores, FP32
+//      accumulation in tensor memory, fused per-query top-CT selection of the cosine
+//      scores straight out of TMEM;
+//   3. merge of the per-CTA partial lists (launch_merge_splits) and exact FP32 re-rank of
+//      the CT candidates with the reference's angular formula (launch_rerank), top-k.
+//
+// tc_scan_kernel is persistent (one CTA per SM) with a stream-K split: the flattened
+// space of (query tile, base tile) pairs is cut into equal contiguous ranges, one per
+// CTA, so every SM gets the same number of MMA tiles; a CTA's range covers at most a few
+// query tiles and emits one partial list per covered tile.  Warp roles:
+//   warp 0  TMA producer (cp.async.bulk.tensor, 128B swizzle, mbarrier complete_tx)
+//   warp 1  MMA issuer (one thread: tcgen05.mma kind::f16, M=128 N=128 K=16 x 8,
+//           tcgen05.commit to mbarriers)
+//   warp 2  TMEM allocator (256 columns = two 128-column FP32 accumulators)
+//   warps 4-7 epilogue: thread r owns query row r (TMEM lane r), reads 32 columns per
+//           tcgen05.ld, skips a 32-column chunk when its maximum does not beat the row's
+//           current CT-th best score, otherwise inserts into a sorted per-row list.
+// Every mbarrier wait is bounded (~2 s of %globaltimer); on timeout the CTA raises the
+// error flag, drains its own in-flight copies and MMAs (bounded again), frees TMEM and
+// returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
 #include "index.h"
+#include "launch_count.h"
+#include "profile.h"
 
 namespace lshg {
 
-void tc_prepare(Index& idx, cudaStream_t s) {
-  (void)idx;
-  (void)s;
-  throw Error(LSHG_ERR_UNSUPPORTED, "tensor-core scan not built yet");
+void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
+
+namespace {
+
+constexpr int BM = 128;                  // queries per tile = UMMA M = TMEM lanes
+constexpr int BN = 128;                  // base points per tile = UMMA N
+constexpr int KD = 128;                  // padded dimension
+constexpr int KHALF = 64;                // bf16 elements per 128-byte swizzle row
+constexpr int HALF_BYTES = BN * KHALF * 2;  // 16 KB
+constexpr int TILE_BYTES = 2 * HALF_BYTES;  // 32 KB
+constexpr int NTHREADS = 256;
+constexpr int TMEM_COLS = 256;
+constexpr uint64_t kWaitNs = 2000000000ull;
+
+struct TcLayout {
+  int stages, ct;
+  int a_off, b_off, sc_off, id_off, bar_off, total;
+};
+
+__host__ __device__ constexpr TcLayout tc_layout(int stages, int ct) {
+  return TcLayout{stages,
+                  ct,
+                  0,
+                  TILE_BYTES,
+                  TILE_BYTES * (1 + stages),
+                  TILE_BYTES * (1 + stages) + ct * BM * 4,
+                  TILE_BYTES * (1 + stages) + ct * BM * 8,
+                  TILE_BYTES * (1 + stages) + ct * BM * 8 + 256 + 1024};
 }
 
-void launch_tc_scan(Index& idx, const float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
-  (void)idx; (void)q; (void)nq; (void)k; (void)out; (void)s;
-  throw Error(LSHG_ERR_UNSUPPORTED, "tensor-core scan not built yet");
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait; gives up when another role aborted (unless `ignore_abort`) or after
+// kWaitNs, raising the abort flag.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, bool ignore_abort = false) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (true) {
+    if (mbar_try(bar, parity)) return true;
+    if (!ignore_abort && *abort_flag) return false;
+    if (global_ns() - t0 > kWaitNs) {
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major, M = 128, N = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <int STAGES, int CT>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    tc_scan_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nq,
+                   int64_t n, int QT, int NT, int per, int maxp, uint64_t* __restrict__ part, int* err) {
+  constexpr TcLayout L = tc_layout(STAGES, CT);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t s0 = smem_u32(sm);
+  float* lsc = reinterpret_cast<float*>(sm + L.sc_off);
+  int* lid = reinterpret_cast<int*>(sm + L.id_off);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + L.bar_off);
+  const uint32_t bar0 = smem_u32(bars);
+  auto FULL = [&](int s) { return bar0 + 8u * s; };
+  auto EMPTY = [&](int s) { return bar0 + 8u * (STAGES + s); };
+  const uint32_t A_FULL = bar0 + 8u * (2 * STAGES);
+  const uint32_t A_EMPTY = A_FULL + 8;
+  auto ACC_FULL = [&](int b) { return bar0 + 8u * (2 * STAGES + 2 + b); };
+  auto ACC_EMPTY = [&](int b) { return bar0 + 8u * (2 * STAGES + 4 + b); };
+  const uint32_t DONE = bar0 + 8u * (2 * STAGES + 6);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 7);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int total = QT * NT;
+  const int t_begin = blockIdx.x * per;
+  const int t_end = min(total, t_begin + per);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(FULL(s), 1);
+      mbar_init(EMPTY(s), 1);
+    }
+    mbar_init(A_FULL, 1);
+    mbar_init(A_EMPTY, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(ACC_FULL(b), 1);
+      mbar_init(ACC_EMPTY(b), 4);
+    }
+    mbar_init(DONE, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int cur_qt = -1, a_round = 0, it = 0;
+      for (int t = t_begin; t < t_end; ++t) {
+        const int qt = t / NT, dt = t - qt * NT;
+        if (qt != cur_qt) {
+          if (!mbar_wait(A_EMPTY, (a_round & 1) ^ 1, abort_flag)) break;
+          mbar_expect_tx(A_FULL, TILE_BYTES);
+          tma_load_2d(s0 + L.a_off, &mapA, 0, qt * BM, A_FULL);
+          tma_load_2d(s0 + L.a_off + HALF_BYTES, &mapA, KHALF, qt * BM, A_FULL);
+          cur_qt = qt;
+          ++a_round;
+        }
+        const int st = it % STAGES, rd = it / STAGES;
+        if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) break;
+        const uint32_t dst = s0 + L.b_off + st * TILE_BYTES;
+        mbar_expect_tx(FULL(st), TILE_BYTES);
+        tma_load_2d(dst, &mapB, 0, dt * BN, FULL(st));
+        tma_load_2d(dst + HALF_BYTES, &mapB, KHALF, dt * BN, FULL(st));
+        ++it;
+      }
+      // drain: every issued copy has landed before the CTA may exit
+      for (int j = max(0, it - STAGES); j < it; ++j) mbar_wait(FULL(j % STAGES), (j / STAGES) & 1, abort_flag, true);
+      if (a_round > 0) mbar_wait(A_FULL, (a_round - 1) & 1, abort_flag, true);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int cur_qt = -1, a_round = 0, it = 0;
+      int use[2] = {0, 0};
+      for (int t = t_begin; t < t_end; ++t) {
+        const int qt = t / NT;
+        if (qt != cur_qt) {
+          if (!mbar_wait(A_FULL, a_round & 1, abort_flag)) break;
+          tc_fence_after();
+          cur_qt = qt;
+          ++a_round;
+        }
+        const int b = it & 1;
+        if (!mbar_wait(ACC_EMPTY(b), (use[b] & 1) ^ 1, abort_flag)) break;
+        tc_fence_after();
+        const int st = it % STAGES, rd = it / STAGES;
+        if (!mbar_wait(FULL(st), rd & 1, abort_flag)) break;
+        tc_fence_after();
+        const uint32_t d_tmem = tmem + (uint32_t)(b * BN);
+        const uint32_t a_base = s0 + L.a_off;
+        const uint32_t b_base = s0 + L.b_off + st * TILE_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < KD / 16; ++kk) {
+          const uint32_t off = (kk >> 2) * HALF_BYTES + (kk & 3) * 32;
+          umma_bf16(d_tmem, smem_desc(a_base + off), smem_desc(b_base + off), kk > 0 ? 1u : 0u);
+        }
+        umma_commit(EMPTY(st));
+        umma_commit(ACC_FULL(b));
+        const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
+        if (last_of_qt) umma_commit(A_EMPTY);
+        ++use[b];
+        ++it;
+      }
+      // drain: all issued MMAs complete before TMEM is released
+      umma_commit(DONE);
+      mbar_wait(DONE, 0, abort_flag, true);
+    }
+    __syncwarp();
+  } else if (warp >= 4) {
+    // ---------------- epilogue: per-row top-CT ----------------
+    const int r = threadIdx.x - 128;  // query row within the tile == TMEM lane
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    for (int i = 0; i < CT; ++i) {
+      lsc[i * BM + r] = -INFINITY;
+      lid[i * BM + r] = -1;
+    }
+    float thr = -INFINITY;
+    int it = 0;
+    int use[2] = {0, 0};
+    for (int t = t_begin; t < t_end; ++t) {
+      const int qt = t / NT, dt = t - qt * NT;
+      const int b = it & 1;
+      if (!mbar_wait(ACC_FULL(b), use[b] & 1, abort_flag)) break;
+      tc_fence_after();
+      const int64_t pbase = (int64_t)dt * BN;
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t v[32];
+        tmem_ld32(tmem + lane_base + (uint32_t)(b * BN + c * 32), v);
+        float mx = __uint_as_float(v[0]);
+#pragma unroll
+        for (int j = 1; j < 32; ++j) mx = fmaxf(mx, __uint_as_float(v[j]));
+        if (mx > thr) {
+#pragma unroll 1
+          for (int j = 0; j < 32; ++j) {
+            const float s = __uint_as_float(v[j]);
+            const int64_t pid = pbase + c * 32 + j;
+            if (s > thr && pid < n) {
+              int pos = CT - 1;
+              while (pos > 0 && lsc[(pos - 1) * BM + r] < s) {
+                lsc[pos * BM + r] = lsc[(pos - 1) * BM + r];
+                lid[pos * BM + r] = lid[(pos - 1) * BM + r];
+                --pos;
+              }
+              lsc[pos * BM + r] = s;
+              lid[pos * BM + r] = (int)pid;
+              thr = lsc[(CT - 1) * BM + r];
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(ACC_EMPTY(b));
+      ++use[b];
+      ++it;
+      const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
+      if (last_of_qt) {
+        const int q = qt * BM + r;
+        if (q < nq) {
+          const int slot = blockIdx.x - (int)(((int64_t)qt * NT) / per);
+          uint64_t* dst = part + ((int64_t)q * maxp + slot) * CT;
+          for (int i = 0; i < CT; ++i) {
+            const int id = lid[i * BM + r];
+            dst[i] = id < 0 ? kEmptyKey : make_key(-lsc[i * BM + r], id);
+          }
+        }
+        for (int i = 0; i < CT; ++i) {
+          lsc[i * BM + r] = -INFINITY;
+          lid[i * BM + r] = -1;
+        }
+        thr = -INFINITY;
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 2);
+}
+
+// Unit rows in BF16, zero-padded to KD columns and to `rows_pad` rows.
+__global__ void to_unit_bf16_kernel(const float* __restrict__ x, int64_t n, int d, int64_t rows_pad,
+                                    __nv_bfloat16* __restrict__ out) {
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < rows_pad; i += nw) {
+    float ss = 0.0f;
+    if (i < n)
+      for (int j = lane; j < d; j += 32) ss = fmaf(x[i * d + j], x[i * d + j], ss);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    const float inv = ss > 0.0f ? rsqrtf(ss) : 0.0f;
+    for (int j = lane; j < KD; j += 32) {
+      float v = (i < n && j < d) ? x[i * d + j] * inv : 0.0f;
+      out[i * KD + j] = __float2bfloat16_rn(v);
+    }
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    LSHG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) throw Error(LSHG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+// Rows of KD bf16 (256 B); boxes of 64 columns x 128 rows with 128-byte swizzle.
+CUtensorMap make_map(const void* base, int64_t rows) {
+  LSHG_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {(cuuint64_t)KD, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)KD * 2};
+  cuuint32_t box[2] = {(cuuint32_t)KHALF, (cuuint32_t)BM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(LSHG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+void to_unit_bf16(const float* x, int64_t n, int d, int64_t rows_pad, uint16_t* out, cudaStream_t s) {
+  int64_t warps = rows_pad;
+  int blocks = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms() * 16);
+  to_unit_bf16_kernel<<<std::max(blocks, 1), 256, 0, s>>>(x, n, d, rows_pad, reinterpret_cast<__nv_bfloat16*>(out));
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+template <int STAGES, int CT>
+void run_kernel(const CUtensorMap& ma, const CUtensorMap& mb, int nq, int64_t n, int QT, int NT, int grid, int per,
+                int maxp, uint64_t* part, int* err, cudaStream_t s) {
+  constexpr TcLayout L = tc_layout(STAGES, CT);
+  auto kern = tc_scan_kernel<STAGES, CT>;
+  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total));
+  ProfScope _ps("tc_scan", s);
+  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, nq, n, QT, NT, per, maxp, part, err);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void tc_prepare(Index& I, cudaStream_t s) {
+  LSHG_REQUIRE(I.dist == DIST_ANGULAR, "tensor-core scan: angular distance only");
+  LSHG_REQUIRE(I.d <= KD, "tensor-core scan: dimension must be <= 128");
+  I.dp = KD;
+  const int64_t npad = (int64_t)ceil_div(I.n, BN) * BN;
+  I.xbf.alloc((size_t)npad * KD, s);
+  to_unit_bf16(I.x.ptr, I.n, I.d, npad, I.xbf.ptr, s);
+}
+
+void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
+  if (nq <= 0) return;
+  LSHG_REQUIRE(k <= 128, "tensor-core scan: k must be <= 128");
+  const int CT = k <= 64 ? 64 : 128;
+  const int64_t qpad = (int64_t)ceil_div(nq, BM) * BM;
+  const int64_t npad = (int64_t)ceil_div(I.n, BN) * BN;
+  const int QT = (int)(qpad / BM), NT = (int)(npad / BN);
+  LSHG_REQUIRE((int64_t)QT * NT < (int64_t)INT_MAX, "tensor-core scan: problem too large");
+  DevBuf<uint16_t> qbf((size_t)qpad * KD, s);
+  to_unit_bf16(q, nq, I.d, qpad, qbf.ptr, s);
+  const CUtensorMap ma = make_map(qbf.ptr, qpad);
+  const CUtensorMap mb = make_map(I.xbf.ptr, npad);
+  const int total = QT * NT;
+  int grid = std::min(num_sms(), total);
+  const int per = ceil_div(total, grid);
+  grid = ceil_div(total, per);
+  const int maxp = ceil_div(NT, per) + 1;
+  DevBuf<uint64_t> part((size_t)nq * maxp * CT, s);
+  LSHG_CUDA(cudaMemsetAsync(part.ptr, 0xff, part.bytes(), s));
+  if (CT == 64) run_kernel<3, 64>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
+  else run_kernel<2, 128>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
+  DevBuf<uint64_t> cand((size_t)nq * CT, s);
+  launch_merge_splits(part.ptr, nq, maxp, CT, cand.ptr, s);
+  // exact FP32 re-rank with the reference's angular formula
+  DevBuf<float> qn((size_t)nq, s);
+  launch_row_norms(q, nq, I.d, qn.ptr, s);
+  launch_rerank(cand.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s);
 }
 
 }  // namespace lshg
