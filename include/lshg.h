@@ -175,6 +175,11 @@ int lshg_merge_topk(const lshg_point* lists, int shards, int N_query, int k_in, 
 int lshg_validate(const lshg_point* truth, int truth_k, const lshg_point* results, int N_query, int k,
                   int reportK, float* recall, float* distance_ratio);
 
+/* Read a GoldStandard truth file (goldstandard.cpp:123-134 writes it; validation.cpp:62-107
+ * reads it): "n\nk\n" then per query "qid:" and k lines "id distance".  Returns a
+ * malloc'ed lshg_point[n*k] (free with lshg_free). */
+int lshg_read_truth(const char* path, int* n, int* k, lshg_point** out);
+
 /* ---- reference text dataset format (gloveparser.cu:9-86, DataParsing/Writer) ------- */
 /* parseFile: returns a malloc'ed float[n*d] (free with lshg_free). */
 int lshg_parse_file(const char* path, int* n, int* d, float** out);

@@ -101,6 +101,7 @@ _SIGS = {
     "lshg_parse_file": (c_int, [c_char_p, C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.POINTER(c_float))]),
     "lshg_write_file": (c_int, [c_char_p, P, c_int, c_int]),
     "lshg_free": (None, [P]),
+    "lshg_read_truth": (c_int, [c_char_p, C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.POINTER(Point))]),
     "lshg_server_params_default": (None, [C.POINTER(ServerParams)]),
     "lshg_server_create": (c_int, [C.POINTER(ServerParams), C.POINTER(c_void_p)]),
     "lshg_server_add_index": (c_int, [P, c_int, P]),

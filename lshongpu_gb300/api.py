@@ -281,6 +281,28 @@ def parse_file(path: str) -> np.ndarray:
     return arr.reshape(n.value, d.value)
 
 
+def read_truth(path: str) -> np.ndarray:
+    """GoldStandard truth file -> (n, k) POINT_DTYPE (validation.cpp:62-107)."""
+    n, k = C.c_int(), C.c_int()
+    ptr = C.POINTER(Point)()
+    check(lib().lshg_read_truth(path.encode(), C.byref(n), C.byref(k), C.byref(ptr)))
+    try:
+        raw = C.string_at(ptr, n.value * k.value * 8) if n.value * k.value else b""
+    finally:
+        lib().lshg_free(ptr)
+    return np.frombuffer(raw, dtype=POINT_DTYPE).reshape(n.value, k.value).copy()
+
+
+def write_truth(path: str, truth: np.ndarray) -> None:
+    """Write (n, k) points in the GoldStandard truth format (goldstandard.cpp:123-134)."""
+    with open(path, "w") as f:
+        f.write(f"{truth.shape[0]}\n{truth.shape[1]}\n")
+        for q, row in enumerate(truth):
+            f.write(f"{q}:\n")
+            for p in row:
+                f.write(f"{int(p['ID'])} {float(p['distance']):.9g}\n")
+
+
 def write_file(path: str, x) -> None:
     x = _f32(x)
     check(lib().lshg_write_file(path.encode(), _ptr(x), x.shape[0], x.shape[1]))
@@ -344,5 +366,5 @@ __all__ = [
     "make_options", "launch_count", "profile_enable", "profile_report", "IMPL_EXACT", "IMPL_SIMHASH", "IMPL_WMH",
     "IMPL_WMH_ONEBIT", "IMPL_JL", "IMPL_TC", "KEYS_SIMHASH", "KEYS_WMH", "KEYS_WMH_ONEBIT", "KEYS_CROSSPOLY",
     "ANGULAR", "JACCARD", "EUCLIDEAN", "EXPORT_DATA", "EXPORT_SKETCHES", "EXPORT_KEYS", "EXPORT_OFFSETS",
-    "EXPORT_BUCKETS", "POINT_DTYPE",
+    "EXPORT_BUCKETS", "POINT_DTYPE", "read_truth", "write_truth",
 ]

@@ -94,6 +94,15 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, out)
+    # knn-compatible command line, linked against the library (rpath $ORIGIN)
+    cli_src = os.path.join(HERE, "cli", "lshg_knn.cpp")
+    cli = os.path.join(LIBDIR, "lshg_knn")
+    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), "-o", cli + ".tmp", cli_src,
+           "-L" + LIBDIR, "-llshg", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(cli + ".tmp", cli)
     # drop stale objects of earlier source versions
     keep = {os.path.basename(o) for o in objs}
     for f in os.listdir(OBJDIR):

@@ -503,4 +503,34 @@ int lshg_write_file(const char* path, const float* x, int n, int d) {
 
 void lshg_free(void* p) { free(p); }
 
+int lshg_read_truth(const char* path, int* n_out, int* k_out, lshg_point** out) {
+  return guarded([&] {
+    LSHG_REQUIRE(path && n_out && k_out && out, "NULL argument");
+    std::ifstream f(path);
+    if (!f) throw Error(LSHG_ERR_IO, std::string("cannot open ") + path);
+    int n = 0, k = 0;
+    f >> n >> k;
+    if (!f || n < 0 || k < 0) throw Error(LSHG_ERR_IO, "bad truth-file header");
+    lshg_point* pts = (lshg_point*)malloc(sizeof(lshg_point) * ((size_t)n * k + 1));
+    std::string qid;
+    for (int q = 0; q < n; ++q) {
+      f >> qid;
+      for (int i = 0; i < k; ++i) {
+        int id = 0;
+        float dist = 0;
+        f >> id >> dist;
+        pts[(size_t)q * k + i].ID = id;
+        pts[(size_t)q * k + i].distance = dist;
+      }
+    }
+    if (!f) {
+      free(pts);
+      throw Error(LSHG_ERR_IO, "truncated truth file");
+    }
+    *n_out = n;
+    *k_out = k;
+    *out = pts;
+  });
+}
+
 }  // extern "C"

@@ -48,9 +48,11 @@ constexpr int NTHREADS = 256;
 constexpr int TMEM_COLS = 256;
 constexpr uint64_t kWaitNs = 2000000000ull;
 
+constexpr int BUFN = 32;  // per-row append buffer (candidates awaiting a warp fold)
+
 struct TcLayout {
   int stages, ct;
-  int a_off, b_off, sc_off, id_off, bar_off, total;
+  int a_off, b_off, sc_off, id_off, bsc_off, bid_off, bar_off, total;
 };
 
 __host__ __device__ constexpr TcLayout tc_layout(int stages, int ct) {
@@ -61,7 +63,85 @@ __host__ __device__ constexpr TcLayout tc_layout(int stages, int ct) {
                   TILE_BYTES * (1 + stages),
                   TILE_BYTES * (1 + stages) + ct * BM * 4,
                   TILE_BYTES * (1 + stages) + ct * BM * 8,
-                  TILE_BYTES * (1 + stages) + ct * BM * 8 + 256 + 1024};
+                  TILE_BYTES * (1 + stages) + ct * BM * 8 + BUFN * BM * 4,
+                  TILE_BYTES * (1 + stages) + ct * BM * 8 + BUFN * BM * 8,
+                  TILE_BYTES * (1 + stages) + ct * BM * 8 + BUFN * BM * 8 + 256 + 1024};
+}
+
+// Row lists and append buffers are stored entry-major ([entry][row]) with the row index
+// XOR-swizzled by the entry index, so both access patterns are bank-conflict free: one
+// lane per row (appends, write-out) and one warp per row (folds).
+__device__ __forceinline__ int sw(int entry, int row) { return entry * BM + (row ^ (entry & 31)); }
+
+// (score, id) order: higher score first, then lower id.
+__device__ __forceinline__ bool better(float as, int ai, float bs, int bi) {
+  return as > bs || (as == bs && ai < bi);
+}
+
+// Fold the append buffer of row `rr` (cnt entries) into its sorted list of 32*E entries.
+// Executed by the whole warp; returns the row's new threshold (its last list entry).
+template <int E>
+__device__ __forceinline__ float warp_fold_row(float* lsc, int* lid, const float* bsc, const int* bid, int rr, int cnt,
+                                               int lane) {
+  // 1. sort the buffer (one entry per lane) descending with a 32-wide bitonic network
+  float bs = lane < cnt ? bsc[sw(lane, rr)] : -INFINITY;
+  int bi = lane < cnt ? bid[sw(lane, rr)] : INT_MAX;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      float os = __shfl_xor_sync(0xffffffffu, bs, j);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, j);
+      bool desc = (lane & k) == 0 || k == 32;
+      bool lower = (lane & j) == 0;
+      bool take = (lower == desc) ? better(os, oi, bs, bi) : better(bs, bi, os, oi);
+      if (take) { bs = os; bi = oi; }
+    }
+  }
+  // 2. list element e*32 + lane; first bitonic-merge stage against the reversed buffer
+  float ls[E];
+  int li[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    ls[e] = lsc[sw(e * 32 + lane, rr)];
+    li[e] = lid[sw(e * 32 + lane, rr)];
+  }
+  {
+    float rs = __shfl_sync(0xffffffffu, bs, 31 - lane);
+    int ri = __shfl_sync(0xffffffffu, bi, 31 - lane);
+    if (better(rs, ri, ls[E - 1], li[E - 1])) { ls[E - 1] = rs; li[E - 1] = ri; }
+  }
+  // 3. bitonic merge (descending) of the 32*E list
+#pragma unroll
+  for (int st = E / 2; st > 0; st >>= 1) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if ((e & st) == 0) {
+        if (better(ls[e | st], li[e | st], ls[e], li[e])) {
+          float ts = ls[e]; int ti = li[e];
+          ls[e] = ls[e | st]; li[e] = li[e | st];
+          ls[e | st] = ts; li[e | st] = ti;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    bool lower = (lane & j) == 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      float os = __shfl_xor_sync(0xffffffffu, ls[e], j);
+      int oi = __shfl_xor_sync(0xffffffffu, li[e], j);
+      bool take = lower ? better(os, oi, ls[e], li[e]) : better(ls[e], li[e], os, oi);
+      if (take) { ls[e] = os; li[e] = oi; }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    lsc[sw(e * 32 + lane, rr)] = ls[e];
+    lid[sw(e * 32 + lane, rr)] = li[e];
+  }
+  return __shfl_sync(0xffffffffu, ls[E - 1], 31);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -144,8 +224,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 template <int STAGES, int CT>
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -269,13 +349,53 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     __syncwarp();
   } else if (warp >= 4) {
     // ---------------- epilogue: per-row top-CT ----------------
+    // Lanes append candidates that beat their row's threshold to the row's buffer; the
+    // warp folds full buffers into the sorted row lists (warp_fold_row) and the
+    // thresholds tighten.  Thresholds may lag between folds; that only admits extra
+    // candidates, never drops one.
     const int r = threadIdx.x - 128;  // query row within the tile == TMEM lane
+    const int row0 = r - lane;
     const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    float* bsc = reinterpret_cast<float*>(sm + L.bsc_off);
+    int* bid = reinterpret_cast<int*>(sm + L.bid_off);
     for (int i = 0; i < CT; ++i) {
-      lsc[i * BM + r] = -INFINITY;
-      lid[i * BM + r] = -1;
+      lsc[sw(i, r)] = -INFINITY;
+      lid[sw(i, r)] = INT_MAX;
     }
+    __syncwarp();
     float thr = -INFINITY;
+    int cnt = 0;
+    auto fold_all = [&](int limit) {
+      unsigned m = __ballot_sync(0xffffffffu, cnt > limit);
+      while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const int c_src = __shfl_sync(0xffffffffu, cnt, src);
+        const float nt = warp_fold_row<CT / 32>(lsc, lid, bsc, bid, row0 + src, c_src, lane);
+        if (lane == src) { thr = nt; cnt = 0; }
+      }
+      __syncwarp();
+    };
+    auto process = [&](const uint32_t (&v)[32], int64_t cbase) {
+      float mx = __uint_as_float(v[0]);
+#pragma unroll
+      for (int j = 1; j < 32; ++j) mx = fmaxf(mx, __uint_as_float(v[j]));
+      if (!__any_sync(0xffffffffu, mx > thr)) return;
+#pragma unroll
+      for (int g = 0; g < 4; ++g) {
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          const int j = g * 8 + jj;
+          const float s = __uint_as_float(v[j]);
+          if (s > thr && cbase + j < n) {
+            bsc[sw(cnt, r)] = s;
+            bid[sw(cnt, r)] = (int)(cbase + j);
+            ++cnt;
+          }
+        }
+        if (__any_sync(0xffffffffu, cnt > BUFN - 8)) fold_all(0);
+      }
+    };
     int it = 0;
     int use[2] = {0, 0};
     for (int t = t_begin; t < t_end; ++t) {
@@ -284,52 +404,42 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!mbar_wait(ACC_FULL(b), use[b] & 1, abort_flag)) break;
       tc_fence_after();
       const int64_t pbase = (int64_t)dt * BN;
-#pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
-        uint32_t v[32];
-        tmem_ld32(tmem + lane_base + (uint32_t)(b * BN + c * 32), v);
-        float mx = __uint_as_float(v[0]);
-#pragma unroll
-        for (int j = 1; j < 32; ++j) mx = fmaxf(mx, __uint_as_float(v[j]));
-        if (mx > thr) {
-#pragma unroll 1
-          for (int j = 0; j < 32; ++j) {
-            const float s = __uint_as_float(v[j]);
-            const int64_t pid = pbase + c * 32 + j;
-            if (s > thr && pid < n) {
-              int pos = CT - 1;
-              while (pos > 0 && lsc[(pos - 1) * BM + r] < s) {
-                lsc[pos * BM + r] = lsc[(pos - 1) * BM + r];
-                lid[pos * BM + r] = lid[(pos - 1) * BM + r];
-                --pos;
-              }
-              lsc[pos * BM + r] = s;
-              lid[pos * BM + r] = (int)pid;
-              thr = lsc[(CT - 1) * BM + r];
-            }
-          }
-        }
-      }
+      const uint32_t ta = tmem + lane_base + (uint32_t)(b * BN);
+      uint32_t va[32], vb[32];
+      tmem_ld32(ta + 0, va);
+      tmem_wait_ld();
+      tmem_ld32(ta + 32, vb);
+      process(va, pbase + 0);
+      tmem_wait_ld();
+      tmem_ld32(ta + 64, va);
+      process(vb, pbase + 32);
+      tmem_wait_ld();
+      tmem_ld32(ta + 96, vb);
+      process(va, pbase + 64);
+      tmem_wait_ld();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(ACC_EMPTY(b));
+      if (lane == 0) mbar_arrive(ACC_EMPTY(b));  // TMEM buffer free: the MMA may overwrite it
+      process(vb, pbase + 96);
       ++use[b];
       ++it;
       const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
       if (last_of_qt) {
+        fold_all(0);
         const int q = qt * BM + r;
         if (q < nq) {
           const int slot = blockIdx.x - (int)(((int64_t)qt * NT) / per);
           uint64_t* dst = part + ((int64_t)q * maxp + slot) * CT;
           for (int i = 0; i < CT; ++i) {
-            const int id = lid[i * BM + r];
-            dst[i] = id < 0 ? kEmptyKey : make_key(-lsc[i * BM + r], id);
+            const int id = lid[sw(i, r)];
+            dst[i] = id == INT_MAX ? kEmptyKey : make_key(-lsc[sw(i, r)], id);
           }
         }
         for (int i = 0; i < CT; ++i) {
-          lsc[i * BM + r] = -INFINITY;
-          lid[i * BM + r] = -1;
+          lsc[sw(i, r)] = -INFINITY;
+          lid[sw(i, r)] = INT_MAX;
         }
+        __syncwarp();
         thr = -INFINITY;
       }
     }
@@ -442,7 +552,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   DevBuf<uint64_t> part((size_t)nq * maxp * CT, s);
   LSHG_CUDA(cudaMemsetAsync(part.ptr, 0xff, part.bytes(), s));
   if (CT == 64) run_kernel<3, 64>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
-  else run_kernel<2, 128>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
+  else run_kernel<1, 128>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
   DevBuf<uint64_t> cand((size_t)nq * CT, s);
   launch_merge_splits(part.ptr, nq, maxp, CT, cand.ptr, s);
   // exact FP32 re-rank with the reference's angular formula
