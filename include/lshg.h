@@ -148,6 +148,18 @@ int lshg_index_build(const lshg_index_params* p, const float* data, int64_t N_da
 int lshg_index_query(lshg_index* idx, const float* queries, int N_query, int k, lshg_point* results,
                      int on_device, void* stream);
 int lshg_index_free(lshg_index* idx);
+/* Allocation-free query (no counterpart in the reference).  For callers that cannot
+ * allocate device memory while answering queries -- e.g. a server whose free HBM is
+ * already held by another allocator, or a latency-critical thread that must not enter
+ * the CUDA allocator.  Serves exact angular linear-scan indexes (implementation 2,
+ * framework 0) only; d_queries [N_query][d] and d_results [N_query][k] are device
+ * pointers.  All temporaries live in one 32 MiB device array per GPU that stays
+ * allocated until the process exits; batches needing more are rejected with
+ * LSHG_ERR_INVALID_ARGUMENT.  Calls that overlap on the GPU race on that array, so
+ * serialise them.  The first call on a device looks up the array's address; make it
+ * before any stream capture begins.  Asynchronous on `stream` (NULL = index stream). */
+int lshg_index_query_noalloc(lshg_index* idx, const float* d_queries, int N_query, int k, lshg_point* d_results,
+                             void* stream);
 
 /* Export index internals to host memory for checks and persistence.  what:
  *  0 = base data after preprocessing (float [n][d])

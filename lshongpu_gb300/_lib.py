@@ -92,6 +92,7 @@ _SIGS = {
     "lshg_index_build": (c_int, [C.POINTER(IndexParams), P, c_int64, c_int, C.POINTER(c_void_p)]),
     "lshg_index_query": (c_int, [P, P, c_int, c_int, P, c_int, P]),
     "lshg_index_free": (c_int, [P]),
+    "lshg_index_query_noalloc": (c_int, [P, P, c_int, c_int, P, P]),
     "lshg_index_export": (c_int, [P, c_int, P, C.POINTER(c_size_t)]),
     "lshg_index_sketch_queries": (c_int, [P, P, c_int, P, P]),
     "lshg_index_save": (c_int, [P, c_char_p]),

@@ -33,6 +33,15 @@ namespace {
 
 thread_local std::string g_last_error;
 
+}  // namespace
+
+namespace lshg {
+// Lets entry points defined in other translation units report their message.
+void set_last_error(const char* msg) { g_last_error = msg; }
+}  // namespace lshg
+
+namespace {
+
 template <typename F>
 int guarded(F&& f) {
   try {
