@@ -45,7 +45,8 @@ constexpr int KHALF = 64;                // bf16 elements per 128-byte swizzle r
 constexpr int HALF_BYTES = BN * KHALF * 2;  // 16 KB
 constexpr int TILE_BYTES = 2 * HALF_BYTES;  // 32 KB
 constexpr int NTHREADS = 256;
-constexpr int TMEM_COLS = 256;
+constexpr int NACC = 4;                  // TMEM accumulator buffers of BN columns
+constexpr int TMEM_COLS = NACC * BN;     // 512 = all of TMEM (one CTA per SM)
 constexpr uint64_t kWaitNs = 2000000000ull;
 
 constexpr int BUFN = 32;  // per-row append buffer (candidates awaiting a warp fold)
@@ -81,7 +82,7 @@ __device__ __forceinline__ bool better(float as, int ai, float bs, int bi) {
 // Fold the append buffer of row `rr` (cnt entries) into its sorted list of 32*E entries.
 // Executed by the whole warp; returns the row's new threshold (its last list entry).
 template <int E>
-__device__ __forceinline__ float warp_fold_row(float* lsc, int* lid, const float* bsc, const int* bid, int rr, int cnt,
+__device__ __noinline__ float warp_fold_row(float* lsc, int* lid, const float* bsc, const int* bid, int rr, int cnt,
                                                int lane) {
   // 1. sort the buffer (one entry per lane) descending with a 32-wide bitonic network
   float bs = lane < cnt ? bsc[sw(lane, rr)] : -INFINITY;
@@ -215,22 +216,37 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 64 consecutive TMEM columns of this thread's lane (issue only; complete with tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,"
+      "%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
         "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
+        "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
+        "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
+        "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
+        "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
       : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Three-input maximum (sm_100+ max.f32 with three sources).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
 
 template <int STAGES, int CT>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tc_scan_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nq,
-                   int64_t n, int QT, int NT, int per, int maxp, uint64_t* __restrict__ part, int* err) {
+                   int64_t n, int QT, int NT, int per, int maxp, uint64_t* __restrict__ part, int* err,
+                   int fold_limit) {
   constexpr TcLayout L = tc_layout(STAGES, CT);
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -244,9 +260,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t A_FULL = bar0 + 8u * (2 * STAGES);
   const uint32_t A_EMPTY = A_FULL + 8;
   auto ACC_FULL = [&](int b) { return bar0 + 8u * (2 * STAGES + 2 + b); };
-  auto ACC_EMPTY = [&](int b) { return bar0 + 8u * (2 * STAGES + 4 + b); };
-  const uint32_t DONE = bar0 + 8u * (2 * STAGES + 6);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 7);
+  auto ACC_EMPTY = [&](int b) { return bar0 + 8u * (2 * STAGES + 2 + NACC + b); };
+  const uint32_t DONE = bar0 + 8u * (2 * STAGES + 2 + 2 * NACC);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 3 + 2 * NACC);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
@@ -262,7 +278,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     mbar_init(A_FULL, 1);
     mbar_init(A_EMPTY, 1);
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NACC; ++b) {
       mbar_init(ACC_FULL(b), 1);
       mbar_init(ACC_EMPTY(b), 4);
     }
@@ -312,7 +328,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       int cur_qt = -1, a_round = 0, it = 0;
-      int use[2] = {0, 0};
       for (int t = t_begin; t < t_end; ++t) {
         const int qt = t / NT;
         if (qt != cur_qt) {
@@ -321,8 +336,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           cur_qt = qt;
           ++a_round;
         }
-        const int b = it & 1;
-        if (!mbar_wait(ACC_EMPTY(b), (use[b] & 1) ^ 1, abort_flag)) break;
+        const int b = it % NACC, ub = it / NACC;  // ub-th use of accumulator b
+        if (!mbar_wait(ACC_EMPTY(b), (ub & 1) ^ 1, abort_flag)) break;
         tc_fence_after();
         const int st = it % STAGES, rd = it / STAGES;
         if (!mbar_wait(FULL(st), rd & 1, abort_flag)) break;
@@ -339,7 +354,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         umma_commit(ACC_FULL(b));
         const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
         if (last_of_qt) umma_commit(A_EMPTY);
-        ++use[b];
         ++it;
       }
       // drain: all issued MMAs complete before TMEM is released
@@ -376,52 +390,60 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
       __syncwarp();
     };
-    auto process = [&](const uint32_t (&v)[32], int64_t cbase) {
-      float mx = __uint_as_float(v[0]);
+    // 8-column group of the tile held in registers: append what beats the threshold
+    auto group = [&](const uint32_t (&v)[64], int g, int64_t cbase) {
+      const float gm = max3f(max3f(__uint_as_float(v[8 * g]), __uint_as_float(v[8 * g + 1]),
+                                   __uint_as_float(v[8 * g + 2])),
+                             max3f(__uint_as_float(v[8 * g + 3]), __uint_as_float(v[8 * g + 4]),
+                                   __uint_as_float(v[8 * g + 5])),
+                             fmaxf(__uint_as_float(v[8 * g + 6]), __uint_as_float(v[8 * g + 7])));
+      if (!__any_sync(0xffffffffu, gm > thr)) return;
 #pragma unroll
-      for (int j = 1; j < 32; ++j) mx = fmaxf(mx, __uint_as_float(v[j]));
-      if (!__any_sync(0xffffffffu, mx > thr)) return;
-#pragma unroll
-      for (int g = 0; g < 4; ++g) {
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const int j = g * 8 + jj;
-          const float s = __uint_as_float(v[j]);
-          if (s > thr && cbase + j < n) {
-            bsc[sw(cnt, r)] = s;
-            bid[sw(cnt, r)] = (int)(cbase + j);
-            ++cnt;
-          }
+      for (int jj = 0; jj < 8; ++jj) {
+        const float s = __uint_as_float(v[8 * g + jj]);
+        const int64_t pid = cbase + 8 * g + jj;
+        if (s > thr && pid < n) {
+          bsc[sw(cnt, r)] = s;
+          bid[sw(cnt, r)] = (int)pid;
+          ++cnt;
         }
-        if (__any_sync(0xffffffffu, cnt > BUFN - 8)) fold_all(0);
       }
+      if (__any_sync(0xffffffffu, cnt > BUFN - 8)) fold_all(fold_limit);
+    };
+    auto half_max = [&](const uint32_t (&v)[64]) {
+      float m[22];
+#pragma unroll
+      for (int i = 0; i < 21; ++i)
+        m[i] = max3f(__uint_as_float(v[3 * i]), __uint_as_float(v[3 * i + 1]), __uint_as_float(v[3 * i + 2]));
+      m[21] = __uint_as_float(v[63]);
+#pragma unroll
+      for (int i = 0; i < 7; ++i) m[i] = max3f(m[3 * i], m[3 * i + 1], m[3 * i + 2]);
+      m[7] = m[21];
+      const float a = max3f(m[0], m[1], m[2]), b = max3f(m[3], m[4], m[5]);
+      return max3f(a, b, fmaxf(m[6], m[7]));
     };
     int it = 0;
-    int use[2] = {0, 0};
     for (int t = t_begin; t < t_end; ++t) {
       const int qt = t / NT, dt = t - qt * NT;
-      const int b = it & 1;
-      if (!mbar_wait(ACC_FULL(b), use[b] & 1, abort_flag)) break;
+      const int b = it % NACC, ub = it / NACC;
+      if (!mbar_wait(ACC_FULL(b), ub & 1, abort_flag)) break;
       tc_fence_after();
       const int64_t pbase = (int64_t)dt * BN;
       const uint32_t ta = tmem + lane_base + (uint32_t)(b * BN);
-      uint32_t va[32], vb[32];
-      tmem_ld32(ta + 0, va);
-      tmem_wait_ld();
-      tmem_ld32(ta + 32, vb);
-      process(va, pbase + 0);
-      tmem_wait_ld();
-      tmem_ld32(ta + 64, va);
-      process(vb, pbase + 32);
-      tmem_wait_ld();
-      tmem_ld32(ta + 96, vb);
-      process(va, pbase + 64);
+      uint32_t v0[64], v1[64];
+      tmem_ld64(ta + 0, v0);
+      tmem_ld64(ta + 64, v1);
       tmem_wait_ld();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(ACC_EMPTY(b));  // TMEM buffer free: the MMA may overwrite it
-      process(vb, pbase + 96);
-      ++use[b];
+      if (lane == 0) mbar_arrive(ACC_EMPTY(b));  // scores are in registers: the MMA may reuse the buffer
+      const float tm = fmaxf(half_max(v0), half_max(v1));
+      if (__any_sync(0xffffffffu, tm > thr)) {
+#pragma unroll
+        for (int g = 0; g < 8; ++g) group(v0, g, pbase);
+#pragma unroll
+        for (int g = 0; g < 8; ++g) group(v1, g, pbase + 64);
+      }
       ++it;
       const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
       if (last_of_qt) {
@@ -511,12 +533,13 @@ void to_unit_bf16(const float* x, int64_t n, int d, int64_t rows_pad, uint16_t* 
 
 template <int STAGES, int CT>
 void run_kernel(const CUtensorMap& ma, const CUtensorMap& mb, int nq, int64_t n, int QT, int NT, int grid, int per,
+                int fold_limit,
                 int maxp, uint64_t* part, int* err, cudaStream_t s) {
   constexpr TcLayout L = tc_layout(STAGES, CT);
   auto kern = tc_scan_kernel<STAGES, CT>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total));
   ProfScope _ps("tc_scan", s);
-  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, nq, n, QT, NT, per, maxp, part, err);
+  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, nq, n, QT, NT, per, maxp, part, err, fold_limit);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
@@ -551,8 +574,15 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   const int maxp = ceil_div(NT, per) + 1;
   DevBuf<uint64_t> part((size_t)nq * maxp * CT, s);
   LSHG_CUDA(cudaMemsetAsync(part.ptr, 0xff, part.bytes(), s));
-  if (CT == 64) run_kernel<3, 64>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
-  else run_kernel<1, 128>(ma, mb, nq, I.n, QT, NT, grid, per, maxp, part.ptr, I.qerr.ptr, s);
+  // rows whose append buffer holds more than fold_limit entries are folded when any row
+  // nears a full buffer (must stay <= BUFN - 8); LSHG_TC_FOLD_LIMIT overrides for tuning
+  static const int fold_limit = [] {
+    const char* e = getenv("LSHG_TC_FOLD_LIMIT");
+    int v = e ? atoi(e) : BUFN - 8;
+    return v < 0 ? 0 : (v > BUFN - 8 ? BUFN - 8 : v);
+  }();
+  if (CT == 64) run_kernel<3, 64>(ma, mb, nq, I.n, QT, NT, grid, per, fold_limit, maxp, part.ptr, I.qerr.ptr, s);
+  else run_kernel<1, 128>(ma, mb, nq, I.n, QT, NT, grid, per, fold_limit, maxp, part.ptr, I.qerr.ptr, s);
   DevBuf<uint64_t> cand((size_t)nq * CT, s);
   launch_merge_splits(part.ptr, nq, maxp, CT, cand.ptr, s);
   // exact FP32 re-rank with the reference's angular formula
