@@ -115,10 +115,70 @@ def build_index(L, x, path: str):
 def algorithmic(path: str, prof: dict, nq: int):
     """(kernel, bound, work per launch, unit) for the dominant kernel of the path."""
     if path == "tc":
-        return "tc_scan", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
+        return "tc_filter", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
     if path == "exact":
         return "scan_float", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
     return "scan_bits", "hbm", N_BASE * 128 / 1e9, "GB/s"
+
+
+def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7) -> dict:
+    """Open-loop Poisson arrivals of requests (batch size log-uniform in [1, 4096], k from
+    {10, 32, 100}, index type drawn uniformly) against the continuous-batching server;
+    latency = submit -> results on the host, as stamped by the library."""
+    import threading
+
+    from lshongpu_gb300 import datasets
+
+    rng = np.random.default_rng(seed)
+    pool = datasets.clustered(4096, DIM, seed=9001)
+    srv = L.Server(max_batch=4096, streams=3, use_graphs=True)
+    for i, ix in indexes.items():
+        srv.add_index(i, ix)
+    ids = list(indexes)
+    mean_size = (4096 - 1) / np.log(4096.0)
+    req_rate = rate_qps / mean_size
+    tickets, lat, sizes = [], [], []
+    done = threading.Event()
+
+    def waiter():
+        i = 0
+        while not (done.is_set() and i >= len(tickets)):
+            if i < len(tickets):
+                _, l = srv.wait(tickets[i])
+                lat.append(l / 1e3)
+                i += 1
+            else:
+                time.sleep(0.0005)
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    nxt = t0
+    while nxt - t0 < seconds:
+        now = time.perf_counter()
+        if now < nxt:
+            time.sleep(min(nxt - now, 0.002))
+            continue
+        size = int(np.exp(rng.uniform(0, np.log(4096))))
+        k = int(rng.choice([10, 32, 100]))
+        which = ids[int(rng.integers(0, len(ids)))]
+        off = int(rng.integers(0, 4096 - size + 1))
+        try:
+            tickets.append(srv.submit(which, pool[off:off + size], k))
+            sizes.append(size)
+        except L.LshgError:
+            pass  # refused by admission: counted in stats
+        nxt += rng.exponential(1.0 / req_rate)
+    done.set()
+    th.join()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat_a = np.array(lat)
+    return {"offered_qps": rate_qps, "achieved_qps": sum(sizes) / wall, "requests": len(tickets),
+            "p50_ms": float(np.percentile(lat_a, 50)), "p99_ms": float(np.percentile(lat_a, 99)),
+            "p999_ms": float(np.percentile(lat_a, 99.9)), "launches": st["launches"],
+            "graph_replays": st["graph_replays"], "rejected": st["rejected"]}
 
 
 def run_reference_arm(args, world, rank):
@@ -273,6 +333,16 @@ def main():
         cpu_qps = sample / tcpu
         extras["cpu_baseline"] = {"value": cpu_qps, "unit": "queries/s", "cores": threads, "kind": "port",
                                   "sample": f"{sample} queries x {N_BASE} points (GoldStandard port)"}
+        # serving: the same resident base behind the continuous-batching loop, mixed with
+        # a 1024-bit SimHash index and a cross-polytope LSH index (L=32, K=2) of it
+        if args.path == "tc":
+            serve_ix = {0: idx,
+                        1: L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=1024)),
+                        2: L.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7,
+                                   bucketKeyBits=16, tables=32, options=L.make_options(cp_hashes=2))}
+            extras["serving"] = [serving_run(L, {0: idx}, rate, 3.0) for rate in (50_000, 200_000)]
+            extras["serving_mixed"] = serving_run(L, serve_ix, 20_000, 3.0)
+            extras["latency_ms"] = {k: extras["serving"][-1][k] for k in ("p50_ms", "p99_ms", "p999_ms")}
 
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,

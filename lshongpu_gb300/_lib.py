@@ -125,7 +125,8 @@ class LshgError(RuntimeError):
 
 
 def lib_path() -> str:
-    return _build.lib_path()
+    """The in-tree build, or the library named by LSHG_LIBRARY (an alternate build)."""
+    return os.environ.get("LSHG_LIBRARY") or _build.lib_path()
 
 
 def lib() -> C.CDLL:

@@ -119,6 +119,7 @@ constexpr float kEmptyDistance = 2147483648.0f;
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 int num_sms();
+void keep_pool_memory();  // keep the default mempool's reserve between query batches
 
 template <typename T>
 __host__ __device__ __forceinline__ T imin(T a, T b) { return a < b ? a : b; }

@@ -256,6 +256,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
                                    cudaStream_t s, double* prep_ms, double* build_ms) {
   LSHG_REQUIRE(n >= 1 && p.d >= 1, "empty base or dimension");
   LSHG_REQUIRE(n < (int64_t)INT_MAX, "base too large for 32-bit ids");
+  keep_pool_memory();
   auto idx = std::make_unique<Index>();
   Index& I = *idx;
   I.p = p;

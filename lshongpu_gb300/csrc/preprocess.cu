@@ -6,6 +6,8 @@
 // `m += x*x`), then an IEEE square root, then an IEEE division for normalisation
 // (processingUtils.cuh:48-67, distanceFunctions.cuh:23-40).  Rows are staged through
 // shared memory so global reads stay coalesced while each thread walks its own row.
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "launch_count.h"
@@ -157,6 +159,26 @@ int num_sms() {
     if (sms <= 0) sms = 1;
   }
   return sms;
+}
+
+// Query batches allocate their temporaries (hundreds of MB for large batches) with
+// cudaMallocAsync.  The default pool returns unused memory to the driver at every
+// synchronisation, so each batch would map its temporaries again; keeping what the
+// process has reserved (release threshold = max) makes those allocations free after the
+// first batch.  The pool is per process: nothing outlives it.
+void keep_pool_memory() {
+  static std::mutex mu;
+  static bool done[128] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return;
+  std::lock_guard<std::mutex> g(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = true;
 }
 
 void launch_row_norms(const float* x, int64_t n, int d, float* norms, cudaStream_t s) {

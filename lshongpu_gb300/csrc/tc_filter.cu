@@ -1,0 +1,504 @@
+// Threshold-filter tensor-core scan: the kernels behind implementation 8's main path.
+//
+// Selecting the top-CT cosine scores of every query out of a Q x N BF16 GEMM is done in
+// two GEMM passes that share one persistent tcgen05 pipeline (tc_filter_kernel):
+//
+//   pass 0 (MODE_GROUPMAX) runs on a strided subsample of the base tiles (every S-th) and
+//     writes, per query row, the maximum score of every GW-column group of every sampled
+//     tile.  Each group maximum is the score of a real base point, so the CT-th largest
+//     of them, tau[q] (tau_select_kernel), is a lower bound of the query's true CT-th best
+//     score: every point of the exact top-CT has score >= tau[q].
+//   pass 1 (MODE_FILTER) runs on the whole base.  The epilogue compares each score with
+//     its row's tau and appends the (rare) survivors to the query's candidate array in
+//     global memory with one atomicAdd each; there is no per-row state on chip, so the
+//     epilogue is a 64-wide maximum and a warp vote per tile in the common case.
+//
+// cand_select_kernel then sorts each query's survivors and keeps the first CT keys
+// (score descending, ties by lower id) -- exactly the top-CT by tensor-core score.  A query
+// with more survivors than the candidate array holds (possible only with massive ties,
+// e.g. duplicated points or a zero query) is listed for the exact per-row list kernel in
+// tc_scan.cu, which runs on the device-side list without a host round trip.
+//
+// Work decomposition of tc_filter_kernel: a unit is (query tile, chunk of CH consecutive
+// base positions); units are numbered chunk-major and dealt round-robin to one CTA per
+// SM.  At any moment the CTAs therefore work on the same one or two chunks for different
+// query tiles, so each base tile is read from HBM about once and served from L2 to the
+// other query tiles; the query tile of a unit is double-buffered in shared memory.
+//
+// Warp roles (384 threads): warp 0 TMA producer, warp 1 MMA issuer (one elected thread),
+// warp 2 TMEM allocator (4 accumulators x 128 columns = 512), warp 3 idle, warps 4-11 the
+// epilogue: warpgroup g (warps 4+4g .. 7+4g) reads TMEM columns [64g, 64g+64) of every
+// accumulator, thread (warp & 3) * 32 + lane owns query row = TMEM lane.  Every mbarrier
+// wait is bounded; a CTA that times out raises the error flag, drains its own copies and
+// MMAs, frees TMEM and returns.
+#include "index.h"
+#include "launch_count.h"
+#include "profile.h"
+#include "select.cuh"
+#include "tc_filter.h"
+#include "tc_ptx.cuh"
+
+namespace lshg {
+namespace tc {
+
+namespace {
+
+constexpr int F_THREADS = 384;
+constexpr int F_STAGES = 4;
+constexpr int F_NACC = 4;
+constexpr int F_TMEM_COLS = F_NACC * BN;
+constexpr int F_EPI_WARPS = 8;
+
+constexpr int F_A_OFF = 0;                               // two query tiles
+constexpr int F_B_OFF = 2 * TILE_BYTES;                  // F_STAGES base tiles
+constexpr int F_BAR_OFF = F_B_OFF + F_STAGES * TILE_BYTES;
+constexpr int F_SMEM = F_BAR_OFF + 256 + 1024;           // + barriers + 1 KB alignment slack
+
+struct FilterArgs {
+  int nq;
+  int64_t n;
+  int QT;        // query tiles
+  int NP;        // base positions scanned (tiles NP of them, base tile = p * dstride)
+  int dstride;
+  int CH;        // positions per unit
+  int NCH;       // chunks = ceil(NP / CH)
+  float* gmax;   // MODE_GROUPMAX: [nq][M] group maxima
+  int M;
+  const float* tau;  // MODE_FILTER: per-query threshold (nullptr = keep everything)
+  int* cnt;          // survivors per query
+  uint64_t* cand;    // [nq][cap] survivor keys
+  int cap;
+  int* err;
+};
+
+template <int MODE, int GW>
+__global__ void __launch_bounds__(F_THREADS, 1)
+    tc_filter_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                     const FilterArgs a) {
+  static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column halves");
+  static_assert(GW == 64 || GW == 8, "group width");
+  const int U = a.NCH * a.QT;
+  if ((int)blockIdx.x >= U) return;  // no unit for this CTA: leave before any barrier or TMEM use
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t s0 = smem_u32(sm);
+  const uint32_t bar0 = s0 + F_BAR_OFF;
+  auto FULL = [&](int s) { return bar0 + 8u * s; };
+  auto EMPTY = [&](int s) { return bar0 + 8u * (F_STAGES + s); };
+  auto A_FULL = [&](int s) { return bar0 + 8u * (2 * F_STAGES + s); };
+  auto A_EMPTY = [&](int s) { return bar0 + 8u * (2 * F_STAGES + 2 + s); };
+  auto ACC_FULL = [&](int b) { return bar0 + 8u * (2 * F_STAGES + 4 + b); };
+  auto ACC_EMPTY = [&](int b) { return bar0 + 8u * (2 * F_STAGES + 4 + F_NACC + b); };
+  const uint32_t DONE = bar0 + 8u * (2 * F_STAGES + 4 + 2 * F_NACC);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + F_BAR_OFF + 8 * (2 * F_STAGES + 5 + 2 * F_NACC));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < F_STAGES; ++s) {
+      mbar_init(FULL(s), 1);
+      mbar_init(EMPTY(s), 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(A_FULL(s), 1);
+      mbar_init(A_EMPTY(s), 1);
+    }
+    for (int b = 0; b < F_NACC; ++b) {
+      mbar_init(ACC_FULL(b), 1);
+      mbar_init(ACC_EMPTY(b), F_EPI_WARPS);
+    }
+    mbar_init(DONE, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), F_TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0, ua = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
+        const int qt = u % a.QT, c = u / a.QT;
+        const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
+        const int ab = ua & 1;
+        if (!mbar_wait(A_EMPTY(ab), ((ua >> 1) & 1) ^ 1, abort_flag)) break;
+        mbar_expect_tx(A_FULL(ab), TILE_BYTES);
+        tma_load_2d(s0 + F_A_OFF + ab * TILE_BYTES, &mapA, 0, qt * BM, A_FULL(ab));
+        tma_load_2d(s0 + F_A_OFF + ab * TILE_BYTES + HALF_BYTES, &mapA, KHALF, qt * BM, A_FULL(ab));
+        for (int p = p0; p < p1; ++p) {
+          const int st = it % F_STAGES, rd = it / F_STAGES;
+          if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
+          const uint32_t dst = s0 + F_B_OFF + st * TILE_BYTES;
+          const int row = p * a.dstride * BN;
+          mbar_expect_tx(FULL(st), TILE_BYTES);
+          tma_load_2d(dst, &mapB, 0, row, FULL(st));
+          tma_load_2d(dst + HALF_BYTES, &mapB, KHALF, row, FULL(st));
+          ++it;
+        }
+      }
+      // drain: every issued copy has landed before the CTA may exit
+      for (int j = max(0, it - F_STAGES); j < it; ++j)
+        mbar_wait(FULL(j % F_STAGES), (j / F_STAGES) & 1, abort_flag, true);
+      for (int j = max(0, ua - 2); j < ua; ++j) mbar_wait(A_FULL(j & 1), (j >> 1) & 1, abort_flag, true);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int it = 0, ua = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
+        const int c = u / a.QT;
+        const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
+        const int ab = ua & 1;
+        if (!mbar_wait(A_FULL(ab), (ua >> 1) & 1, abort_flag)) break;
+        tc_fence_after();
+        for (int p = p0; p < p1; ++p) {
+          const int b = it % F_NACC, ub = it / F_NACC;
+          if (!mbar_wait(ACC_EMPTY(b), (ub & 1) ^ 1, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const int st = it % F_STAGES, rd = it / F_STAGES;
+          if (!mbar_wait(FULL(st), rd & 1, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          umma_tile(tmem + (uint32_t)(b * BN), s0 + F_A_OFF + ab * TILE_BYTES, s0 + F_B_OFF + st * TILE_BYTES);
+          umma_commit(EMPTY(st));
+          umma_commit(ACC_FULL(b));
+          ++it;
+        }
+        umma_commit(A_EMPTY(ab));  // the query tile is free once this unit's MMAs complete
+      }
+      // drain: all issued MMAs complete before TMEM is released
+      umma_commit(DONE);
+      mbar_wait(DONE, 0, abort_flag, true);
+    }
+    __syncwarp();
+  } else if (warp >= 4) {
+    // ---------------- epilogue ----------------
+    const int g = (warp - 4) >> 2;               // column half of every accumulator
+    const int r = (warp & 3) * 32 + lane;        // query row within the tile = TMEM lane
+    const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(g * 64);
+    int it = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < U && ok; u += gridDim.x) {
+      const int qt = u % a.QT, c = u / a.QT;
+      const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
+      const int q = qt * BM + r;
+      float tau = INFINITY;
+      if (MODE == MODE_FILTER && q < a.nq) tau = a.tau ? a.tau[q] : -INFINITY;
+      for (int p = p0; p < p1; ++p) {
+        const int b = it % F_NACC, ub = it / F_NACC;
+        if (!mbar_wait(ACC_FULL(b), ub & 1, abort_flag)) { ok = false; break; }
+        tc_fence_after();
+        uint32_t v[64];
+        tmem_ld64(tbase + (uint32_t)(b * BN), v);
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(ACC_EMPTY(b));  // scores are in registers: the MMA may reuse the buffer
+        ++it;
+        const int64_t cbase = (int64_t)p * a.dstride * BN + g * 64;  // base id of v[0]
+        if (MODE == MODE_GROUPMAX) {
+          if (cbase + 64 > a.n) {  // last base tile: padding rows are not points
+#pragma unroll
+            for (int j = 0; j < 64; ++j)
+              if (cbase + j >= a.n) v[j] = __float_as_uint(-INFINITY);
+          }
+          if (q < a.nq) {
+            if (GW == 64) {
+              float m[8];
+#pragma unroll
+              for (int gg = 0; gg < 8; ++gg) m[gg] = max8(v, gg);
+              a.gmax[(int64_t)q * a.M + 2 * p + g] =
+                  max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]), fmaxf(m[6], m[7]));
+            } else {
+              float4 lo, hi;
+              lo.x = max8(v, 0); lo.y = max8(v, 1); lo.z = max8(v, 2); lo.w = max8(v, 3);
+              hi.x = max8(v, 4); hi.y = max8(v, 5); hi.z = max8(v, 6); hi.w = max8(v, 7);
+              float4* dst = reinterpret_cast<float4*>(a.gmax + (int64_t)q * a.M + 16 * p + 8 * g);
+              dst[0] = lo;
+              dst[1] = hi;
+            }
+          }
+        } else {
+          float m[8];
+#pragma unroll
+          for (int gg = 0; gg < 8; ++gg) m[gg] = max8(v, gg);
+          const float tm = max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]), fmaxf(m[6], m[7]));
+          if (__any_sync(0xffffffffu, tm >= tau)) {
+#pragma unroll
+            for (int gg = 0; gg < 8; ++gg) {
+              if (!__any_sync(0xffffffffu, m[gg] >= tau)) continue;
+#pragma unroll
+              for (int jj = 0; jj < 8; ++jj) {
+                const float s = __uint_as_float(v[8 * gg + jj]);
+                const int64_t pid = cbase + 8 * gg + jj;
+                if (s >= tau && pid < a.n) {
+                  const int slot = atomicAdd(a.cnt + q, 1);
+                  if (slot < a.cap) a.cand[(int64_t)q * a.cap + slot] = make_key(-s, (int)pid);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2) {
+    tc_fence_after();
+    tmem_dealloc(tmem, F_TMEM_COLS);
+  }
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(a.err, 2);
+}
+
+// tau[q] = (CT-th largest of the row's M group maxima) - margin, or -inf when the row has
+// fewer than CT finite-or-infinite (non-NaN) maxima.  One warp per query: a 4-pass
+// 8-bit radix select on order-preserving keys, histogram in shared memory.
+__global__ void __launch_bounds__(256) tau_select_kernel(const float* __restrict__ gmax, int nq, int M, int CT,
+                                                          float margin, float* __restrict__ tau) {
+  __shared__ unsigned hist[8][256];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = blockIdx.x * 8 + w;
+  if (q >= nq) return;  // warp-uniform; only __syncwarp below
+  const float* row = gmax + (int64_t)q * M;
+  uint32_t prefix = 0, pmask = 0;
+  int kk = CT;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    for (int i = lane; i < 256; i += 32) hist[w][i] = 0;
+    __syncwarp();
+    for (int i = lane; i < M; i += 32) {
+      const float f = row[i];
+      if (f != f) continue;  // NaN maxima are not scores
+      const uint32_t key = float_to_ordered(f);
+      if ((key & pmask) == prefix) atomicAdd(&hist[w][(key >> shift) & 255u], 1u);
+    }
+    __syncwarp();
+    // lane l owns digits 255-8l .. 248-8l (descending); inclusive prefix over lanes
+    unsigned own = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) own += hist[w][255 - 8 * lane - j];
+    unsigned incl = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total < (unsigned)kk) {  // fewer than CT usable maxima (only possible on the first pass)
+      if (lane == 0) tau[q] = -INFINITY;
+      return;
+    }
+    const unsigned hit = __ballot_sync(0xffffffffu, incl >= (unsigned)kk);
+    const int L = __ffs(hit) - 1;
+    int digit = 0, rem = 0;
+    if (lane == L) {
+      unsigned acc = incl - own;
+      for (int j = 0; j < 8; ++j) {
+        const int d = 255 - 8 * lane - j;
+        const unsigned h = hist[w][d];
+        if (acc + h >= (unsigned)kk) {
+          digit = d;
+          rem = kk - (int)acc;
+          break;
+        }
+        acc += h;
+      }
+    }
+    digit = __shfl_sync(0xffffffffu, digit, L);
+    rem = __shfl_sync(0xffffffffu, rem, L);
+    prefix |= (uint32_t)digit << shift;
+    pmask |= 255u << shift;
+    kk = rem;
+    __syncwarp();
+  }
+  if (lane == 0) tau[q] = ordered_to_float(prefix) - margin;
+}
+
+// Per query: sort the survivors and keep the first CT keys; list queries whose survivors
+// overflowed the candidate array (ovf[0] = count, ovf[1..] = query ids).
+__global__ void cand_select_kernel(const int* __restrict__ cnt, const uint64_t* __restrict__ cand, int cap, int CT,
+                                   uint64_t* __restrict__ out, int* __restrict__ ovf) {
+  extern __shared__ uint64_t ks[];
+  const int q = blockIdx.x;
+  const int c = cnt[q];
+  if (c > cap) {
+    for (int i = threadIdx.x; i < CT; i += blockDim.x) out[(int64_t)q * CT + i] = kEmptyKey;
+    if (threadIdx.x == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
+    return;
+  }
+  int P = CT;
+  while (P < c) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) ks[i] = i < c ? cand[(int64_t)q * cap + i] : kEmptyKey;
+  __syncthreads();
+  block_bitonic_sort(ks, P);
+  for (int i = threadIdx.x; i < CT; i += blockDim.x) out[(int64_t)q * CT + i] = ks[i];
+}
+
+// Compact the bf16 rows of the listed queries into rows 0..count-1 of `dst` (the rest of
+// the last 128-row tile is zeroed).
+__global__ void gather_rows_kernel(const uint16_t* __restrict__ src, const int* __restrict__ ovf,
+                                   uint16_t* __restrict__ dst) {
+  const int cntq = ovf[0];
+  const int64_t rows = (int64_t)((cntq + BM - 1) / BM) * BM;
+  const int64_t chunks = rows * (KD / 8);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < chunks; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / (KD / 8);
+    const int c = (int)(t % (KD / 8));
+    uint4 val = make_uint4(0, 0, 0, 0);
+    if (i < cntq) val = reinterpret_cast<const uint4*>(src + (int64_t)ovf[1 + i] * KD)[c];
+    reinterpret_cast<uint4*>(dst + i * KD)[c] = val;
+  }
+}
+
+// Merge the list kernel's per-CTA partial lists of every listed query and write the
+// result over the query's row of `out`.  The split arithmetic repeats the list kernel's
+// (tc_list_geometry).
+__global__ void merge_fallback_kernel(const uint64_t* __restrict__ part, const int* __restrict__ ovf, int NT,
+                                      int grid, int CT, uint64_t* __restrict__ out) {
+  extern __shared__ uint64_t ms[];
+  const int cntq = ovf[0];
+  if (cntq == 0) return;
+  const ListGeometry geo = tc_list_geometry(cntq, NT, grid);
+  for (int i = blockIdx.x; i < cntq; i += gridDim.x) {
+    const int qt = i / BM;
+    const int first = (int)(((int64_t)qt * NT) / geo.per);
+    const int last = (int)(((int64_t)qt * NT + NT - 1) / geo.per);
+    const uint64_t* src = part + (int64_t)i * geo.maxp * CT;
+    for (int j = threadIdx.x; j < CT; j += blockDim.x) ms[j] = src[j];
+    __syncthreads();
+    for (int s = 1; s <= last - first; ++s) {
+      const uint64_t* lst = src + (int64_t)s * CT;
+      for (int j = threadIdx.x; j < CT; j += blockDim.x) {
+        const uint64_t b = lst[CT - 1 - j];
+        if (b < ms[j]) ms[j] = b;
+      }
+      __syncthreads();
+      block_bitonic_merge(ms, CT);
+    }
+    const int q = ovf[1 + i];
+    for (int j = threadIdx.x; j < CT; j += blockDim.x) out[(int64_t)q * CT + j] = ms[j];
+    __syncthreads();
+  }
+}
+
+template <int MODE, int GW>
+void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, FilterArgs a, const char* name, cudaStream_t s) {
+  // chunk size: long enough to amortise the query-tile switch, short enough for >= 4
+  // units per CTA
+  const int G = num_sms();
+  const int64_t work = (int64_t)a.NP * a.QT;
+  a.CH = (int)std::max<int64_t>(1, std::min<int64_t>(32, (work + 4 * G - 1) / (4 * G)));
+  a.NCH = ceil_div(a.NP, a.CH);
+  const int U = a.NCH * a.QT;
+  const int grid = std::min(G, U);
+  auto kern = tc_filter_kernel<MODE, GW>;
+  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM));
+  ProfScope _ps(name, s);
+  kern<<<grid, F_THREADS, F_SMEM, s>>>(ma, mb, a);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+FilterPlan plan_filter(int64_t n, int CT) {
+  FilterPlan p{};
+  const int NT = ceil_div(n, BN);
+  p.NT = NT;
+  if (NT >= 2 * CT) {
+    p.GW = 64;
+    p.S = (int)std::max<int64_t>(1, std::min<int64_t>(8, NT / (8 * CT)));
+    p.NS = ceil_div(NT, p.S);
+    p.M = 2 * p.NS;
+    p.cap = std::max(1024, 4 * CT * p.S);
+  } else if (NT * 16 >= 4 * CT) {
+    p.GW = 8;
+    p.S = 1;
+    p.NS = NT;
+    p.M = 16 * NT;
+    p.cap = std::max(1024, 4 * CT);
+  } else {  // a few thousand points: keep every one
+    p.GW = 0;
+    p.S = 1;
+    p.NS = 0;
+    p.M = 0;
+    p.cap = NT * BN;
+  }
+  p.cap = std::min<int64_t>(p.cap, (int64_t)NT * BN);
+  return p;
+}
+
+void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const FilterPlan& plan, int nq, int64_t n,
+                        int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s) {
+  FilterArgs a{};
+  a.nq = nq;
+  a.n = n;
+  a.QT = QT;
+  a.err = err;
+  if (plan.M > 0) {
+    DevBuf<float> gmax((size_t)nq * plan.M, s);
+    a.NP = plan.NS;
+    a.dstride = plan.S;
+    a.gmax = gmax.ptr;
+    a.M = plan.M;
+    if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64>(ma, mb, a, "tc_prepass", s);
+    else run_filter<MODE_GROUPMAX, 8>(ma, mb, a, "tc_prepass", s);
+    {
+      ProfScope _ps("tc_tau_select", s);
+      tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, kTauMargin, tau);
+      count_launch();
+      LSHG_CHECK_LAUNCH();
+    }
+  }
+  a.gmax = nullptr;
+  a.M = 0;
+  a.NP = plan.NT;
+  a.dstride = 1;
+  a.tau = plan.M > 0 ? tau : nullptr;
+  a.cnt = cnt;
+  a.cand = cand;
+  a.cap = plan.cap;
+  run_filter<MODE_FILTER, 64>(ma, mb, a, "tc_filter", s);
+}
+
+void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
+                        cudaStream_t s) {
+  int P = CT;
+  while (P < cap) P <<= 1;
+  const size_t smem = (size_t)P * 8;
+  LSHG_REQUIRE(smem <= 200 * 1024, "tensor-core scan: candidate array too large");
+  ProfScope _ps("tc_cand_select", s);
+  LSHG_CUDA(cudaFuncSetAttribute(cand_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cand_select_kernel<<<nq, 256, smem, s>>>(cnt, cand, cap, CT, out, ovf);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_gather_rows(const uint16_t* src, const int* ovf, int nq, uint16_t* dst, cudaStream_t s) {
+  const int64_t chunks = (int64_t)ceil_div(nq, BM) * BM * (KD / 8);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((chunks + 255) / 256, (int64_t)num_sms() * 4));
+  gather_rows_kernel<<<blocks, 256, 0, s>>>(src, ovf, dst);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_merge_fallback(const uint64_t* part, const int* ovf, int nq, int NT, int grid, int CT, uint64_t* out,
+                           cudaStream_t s) {
+  const size_t smem = (size_t)CT * 8;
+  merge_fallback_kernel<<<std::min(nq, num_sms() * 4), 128, smem, s>>>(part, ovf, NT, grid, CT, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+}  // namespace tc
+}  // namespace lshg

@@ -1,0 +1,59 @@
+// Host-side interface of the tensor-core scan kernels (tc_filter.cu, tc_scan.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace lshg {
+namespace tc {
+
+constexpr int MODE_GROUPMAX = 0;  // prepass: per-row group maxima of sampled tiles
+constexpr int MODE_FILTER = 1;    // main pass: keep scores >= the row's threshold
+
+// Subtracted from every threshold: the prepass and the main pass compute each score with
+// the same instruction sequence, so this only guards against a last-bit difference.
+constexpr float kTauMargin = 1e-6f;
+
+// Parameters of the threshold prepass for a base of n points and CT candidates a query.
+struct FilterPlan {
+  int NT;   // base tiles
+  int GW;   // group width of the prepass maxima (64 or 8; 0 = no prepass, keep every point)
+  int S;    // prepass samples every S-th base tile
+  int NS;   // sampled tiles
+  int M;    // group maxima a query row
+  int cap;  // survivor slots a query
+};
+
+FilterPlan plan_filter(int64_t n, int CT);
+
+// Prepass + threshold selection + filter pass: fills cnt[q] and cand[q][0..cap).
+void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const FilterPlan& plan, int nq, int64_t n,
+                        int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s);
+
+// Top-CT keys a query from its survivors; overflowed queries are listed in ovf.
+void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
+                        cudaStream_t s);
+
+void launch_gather_rows(const uint16_t* src, const int* ovf, int nq, uint16_t* dst, cudaStream_t s);
+
+void launch_merge_fallback(const uint64_t* part, const int* ovf, int nq, int NT, int grid, int CT, uint64_t* out,
+                           cudaStream_t s);
+
+// Work split of the per-row list kernel over `rows` gathered query rows: query tiles,
+// tiles a CTA (stream-K), and partial-list slots a row.
+struct ListGeometry {
+  int QT, total, per, maxp;
+};
+__host__ __device__ inline ListGeometry tc_list_geometry(int rows, int NT, int grid) {
+  ListGeometry g;
+  g.QT = (rows + 127) / 128;
+  g.total = g.QT * NT;
+  g.per = g.total > 0 ? (g.total + grid - 1) / grid : 1;
+  g.maxp = (NT + g.per - 1) / g.per + 1;
+  return g;
+}
+
+}  // namespace tc
+}  // namespace lshg

@@ -1,55 +1,52 @@
 // Tensor-core exact scan (implementation 8; no reference counterpart -- it replaces the
 // reference's FP32 exact scan, memOptimizedLinearScan.cu:20-106, for angular k-NN).
 //
-// Pipeline per query batch:
+// Pipeline per query batch (launch_tc_scan):
 //   1. queries -> unit rows in BF16, zero-padded to 128 dims (the base was converted the
 //      same way at build: x / |x|);
-//   2. tc_scan_kernel: BF16 GEMM Q x N on the 5th-generation tensor cores, FP32
-//      accumulation in tensor memory, fused per-query top-CT selection of the cosine
-//      scores straight out of TMEM;
-//   3. merge of the per-CTA partial lists (launch_merge_splits) and exact FP32 re-rank of
-//      the CT candidates with the reference's angular formula (launch_rerank), top-k.
+//   2. threshold prepass + filter pass on the tensor cores (tc_filter.cu): every query
+//      collects the base points whose cosine score reaches a lower bound of its CT-th best
+//      score;
+//   3. cand_select: the top-CT of those survivors by (score desc, id asc);
+//   4. overflow fallback, entirely on the device: queries whose survivors did not fit
+//      their candidate array are gathered and rescanned by tc_list_kernel below, which
+//      keeps an exact per-row top-CT list in shared memory (no thresholds needed);
+//   5. exact FP32 re-rank of the CT candidates with the reference's angular formula
+//      (launch_rerank), top-k.
 //
-// tc_scan_kernel is persistent (one CTA per SM) with a stream-K split: the flattened
-// space of (query tile, base tile) pairs is cut into equal contiguous ranges, one per
-// CTA, so every SM gets the same number of MMA tiles; a CTA's range covers at most a few
-// query tiles and emits one partial list per covered tile.  Warp roles:
+// tc_list_kernel is persistent (one CTA per SM) with a stream-K split of the (query tile,
+// base tile) space; its CTA count and split are derived on the device from the gathered
+// row count, so the fallback costs three near-empty launches when nothing overflowed.
+// Warp roles:
 //   warp 0  TMA producer (cp.async.bulk.tensor, 128B swizzle, mbarrier complete_tx)
-//   warp 1  MMA issuer (one thread: tcgen05.mma kind::f16, M=128 N=128 K=16 x 8,
-//           tcgen05.commit to mbarriers)
-//   warp 2  TMEM allocator (256 columns = two 128-column FP32 accumulators)
-//   warps 4-7 epilogue: thread r owns query row r (TMEM lane r), reads 32 columns per
-//           tcgen05.ld, skips a 32-column chunk when its maximum does not beat the row's
-//           current CT-th best score, otherwise inserts into a sorted per-row list.
+//   warp 1  MMA issuer (one thread: tcgen05.mma kind::f16, M=128 N=128 K=16 x 8)
+//   warp 2  TMEM allocator (four 128-column FP32 accumulators)
+//   warps 4-7 epilogue: thread r owns query row r (TMEM lane r); per tile it loads its
+//           128 scores with two tcgen05.ld .x64, releases the accumulator, filters with
+//           a two-level maximum against the row's threshold, appends survivors to a
+//           per-row buffer and folds nearly full buffers into the sorted per-row top-CT
+//           lists with shuffle bitonic networks (warp_fold_row).
 // Every mbarrier wait is bounded (~2 s of %globaltimer); on timeout the CTA raises the
 // error flag, drains its own in-flight copies and MMAs (bounded again), frees TMEM and
 // returns.
-#include <cuda.h>
-#include <cuda_bf16.h>
-#include <cudaTypedefs.h>
-
 #include "index.h"
 #include "launch_count.h"
 #include "profile.h"
+#include "tc_filter.h"
+#include "tc_ptx.cuh"
 
 namespace lshg {
 
 void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
 
+namespace tc {
+
 namespace {
 
-constexpr int BM = 128;                  // queries per tile = UMMA M = TMEM lanes
-constexpr int BN = 128;                  // base points per tile = UMMA N
-constexpr int KD = 128;                  // padded dimension
-constexpr int KHALF = 64;                // bf16 elements per 128-byte swizzle row
-constexpr int HALF_BYTES = BN * KHALF * 2;  // 16 KB
-constexpr int TILE_BYTES = 2 * HALF_BYTES;  // 32 KB
 constexpr int NTHREADS = 256;
 constexpr int NACC = 4;                  // TMEM accumulator buffers of BN columns
 constexpr int TMEM_COLS = NACC * BN;     // 512 = all of TMEM (one CTA per SM)
-constexpr uint64_t kWaitNs = 2000000000ull;
-
-constexpr int BUFN = 32;  // per-row append buffer (candidates awaiting a warp fold)
+constexpr int BUFN = 32;                 // per-row append buffer (candidates awaiting a warp fold)
 
 struct TcLayout {
   int stages, ct;
@@ -145,109 +142,17 @@ __device__ __noinline__ float warp_fold_row(float* lsc, int* lid, const float* b
   return __shfl_sync(0xffffffffu, ls[E - 1], 31);
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-// Bounded wait; gives up when another role aborted (unless `ignore_abort`) or after
-// kWaitNs, raising the abort flag.
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, bool ignore_abort = false) {
-  if (mbar_try(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  while (true) {
-    if (mbar_try(bar, parity)) return true;
-    if (!ignore_abort && *abort_flag) return false;
-    if (global_ns() - t0 > kWaitNs) {
-      *abort_flag = 1;
-      return false;
-    }
-  }
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major, M = 128, N = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
-
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-          tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-// 64 consecutive TMEM columns of this thread's lane (issue only; complete with tmem_wait_ld).
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
-      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,"
-      "%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
-        "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
-        "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
-        "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
-        "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
-      : "r"(taddr));
-}
-
-// Three-input maximum (sm_100+ max.f32 with three sources).
-__device__ __forceinline__ float max3f(float a, float b, float c) {
-  float r;
-  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-  return r;
-}
 
 template <int STAGES, int CT>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    tc_scan_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nq,
-                   int64_t n, int QT, int NT, int per, int maxp, uint64_t* __restrict__ part, int* err,
-                   int fold_limit) {
+    tc_list_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   const int* __restrict__ rows_dev, int64_t n, int NT, uint64_t* __restrict__ part, int* err) {
   constexpr TcLayout L = tc_layout(STAGES, CT);
+  constexpr int fold_limit = BUFN - 8;
+  const int nq = *rows_dev;  // gathered query rows (0: nothing to do)
+  const ListGeometry geo = tc_list_geometry(nq, NT, gridDim.x);
+  const int QT = geo.QT, per = geo.per, maxp = geo.maxp;
+  if ((int64_t)blockIdx.x * per >= geo.total) return;  // no tiles: leave before any barrier or TMEM use
   extern __shared__ uint8_t smem_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const uint32_t s0 = smem_u32(sm);
@@ -286,12 +191,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 2) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
+  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -342,14 +242,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int st = it % STAGES, rd = it / STAGES;
         if (!mbar_wait(FULL(st), rd & 1, abort_flag)) break;
         tc_fence_after();
-        const uint32_t d_tmem = tmem + (uint32_t)(b * BN);
-        const uint32_t a_base = s0 + L.a_off;
-        const uint32_t b_base = s0 + L.b_off + st * TILE_BYTES;
-#pragma unroll
-        for (int kk = 0; kk < KD / 16; ++kk) {
-          const uint32_t off = (kk >> 2) * HALF_BYTES + (kk & 3) * 32;
-          umma_bf16(d_tmem, smem_desc(a_base + off), smem_desc(b_base + off), kk > 0 ? 1u : 0u);
-        }
+        umma_tile(tmem + (uint32_t)(b * BN), s0 + L.a_off, s0 + L.b_off + st * TILE_BYTES);
         umma_commit(EMPTY(st));
         umma_commit(ACC_FULL(b));
         const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
@@ -471,7 +364,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __syncthreads();
   if (warp == 2) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    tmem_dealloc(tmem, TMEM_COLS);
   }
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, 2);
 }
@@ -496,7 +389,17 @@ __global__ void to_unit_bf16_kernel(const float* __restrict__ x, int64_t n, int 
   }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+void to_unit_bf16(const float* x, int64_t n, int d, int64_t rows_pad, uint16_t* out, cudaStream_t s) {
+  int64_t warps = rows_pad;
+  int blocks = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms() * 16);
+  to_unit_bf16_kernel<<<std::max(blocks, 1), 256, 0, s>>>(x, n, d, rows_pad, reinterpret_cast<__nv_bfloat16*>(out));
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
     cudaDriverEntryPointQueryResult q;
@@ -523,30 +426,24 @@ CUtensorMap make_map(const void* base, int64_t rows) {
   return m;
 }
 
-void to_unit_bf16(const float* x, int64_t n, int d, int64_t rows_pad, uint16_t* out, cudaStream_t s) {
-  int64_t warps = rows_pad;
-  int blocks = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms() * 16);
-  to_unit_bf16_kernel<<<std::max(blocks, 1), 256, 0, s>>>(x, n, d, rows_pad, reinterpret_cast<__nv_bfloat16*>(out));
-  count_launch();
-  LSHG_CHECK_LAUNCH();
-}
+namespace {
 
 template <int STAGES, int CT>
-void run_kernel(const CUtensorMap& ma, const CUtensorMap& mb, int nq, int64_t n, int QT, int NT, int grid, int per,
-                int fold_limit,
-                int maxp, uint64_t* part, int* err, cudaStream_t s) {
+void run_list_kernel(const CUtensorMap& ma, const CUtensorMap& mb, const int* rows_dev, int64_t n, int NT, int grid,
+                     uint64_t* part, int* err, cudaStream_t s) {
   constexpr TcLayout L = tc_layout(STAGES, CT);
-  auto kern = tc_scan_kernel<STAGES, CT>;
+  auto kern = tc_list_kernel<STAGES, CT>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total));
-  ProfScope _ps("tc_scan", s);
-  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, nq, n, QT, NT, per, maxp, part, err, fold_limit);
+  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, rows_dev, n, NT, part, err);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
 
 }  // namespace
+}  // namespace tc
 
 void tc_prepare(Index& I, cudaStream_t s) {
+  using namespace tc;
   LSHG_REQUIRE(I.dist == DIST_ANGULAR, "tensor-core scan: angular distance only");
   LSHG_REQUIRE(I.d <= KD, "tensor-core scan: dimension must be <= 128");
   I.dp = KD;
@@ -556,39 +453,52 @@ void tc_prepare(Index& I, cudaStream_t s) {
 }
 
 void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
+  using namespace tc;
   if (nq <= 0) return;
   LSHG_REQUIRE(k <= 128, "tensor-core scan: k must be <= 128");
   const int CT = k <= 64 ? 64 : 128;
   const int64_t qpad = (int64_t)ceil_div(nq, BM) * BM;
-  const int64_t npad = (int64_t)ceil_div(I.n, BN) * BN;
-  const int QT = (int)(qpad / BM), NT = (int)(npad / BN);
+  const int QT = (int)(qpad / BM);
+  FilterPlan plan = plan_filter(I.n, CT);
+  // test hook: LSHG_TC_FORCE_FALLBACK=1 sends every query through the list kernel, so
+  // tests can compare the two selection paths on the same inputs
+  if (const char* e = getenv("LSHG_TC_FORCE_FALLBACK"); e && e[0] == '1') plan.cap = 0;
+  const int NT = plan.NT;
   LSHG_REQUIRE((int64_t)QT * NT < (int64_t)INT_MAX, "tensor-core scan: problem too large");
   DevBuf<uint16_t> qbf((size_t)qpad * KD, s);
   to_unit_bf16(q, nq, I.d, qpad, qbf.ptr, s);
   const CUtensorMap ma = make_map(qbf.ptr, qpad);
-  const CUtensorMap mb = make_map(I.xbf.ptr, npad);
-  const int total = QT * NT;
-  int grid = std::min(num_sms(), total);
-  const int per = ceil_div(total, grid);
-  grid = ceil_div(total, per);
-  const int maxp = ceil_div(NT, per) + 1;
-  DevBuf<uint64_t> part((size_t)nq * maxp * CT, s);
-  LSHG_CUDA(cudaMemsetAsync(part.ptr, 0xff, part.bytes(), s));
-  // rows whose append buffer holds more than fold_limit entries are folded when any row
-  // nears a full buffer (must stay <= BUFN - 8); LSHG_TC_FOLD_LIMIT overrides for tuning
-  static const int fold_limit = [] {
-    const char* e = getenv("LSHG_TC_FOLD_LIMIT");
-    int v = e ? atoi(e) : BUFN - 8;
-    return v < 0 ? 0 : (v > BUFN - 8 ? BUFN - 8 : v);
-  }();
-  if (CT == 64) run_kernel<3, 64>(ma, mb, nq, I.n, QT, NT, grid, per, fold_limit, maxp, part.ptr, I.qerr.ptr, s);
-  else run_kernel<1, 128>(ma, mb, nq, I.n, QT, NT, grid, per, fold_limit, maxp, part.ptr, I.qerr.ptr, s);
-  DevBuf<uint64_t> cand((size_t)nq * CT, s);
-  launch_merge_splits(part.ptr, nq, maxp, CT, cand.ptr, s);
-  // exact FP32 re-rank with the reference's angular formula
+  const CUtensorMap mb = make_map(I.xbf.ptr, (int64_t)NT * BN);
+
+  // 1-2. thresholds and survivors
+  DevBuf<float> tau((size_t)nq, s);
+  DevBuf<int> cnt((size_t)nq + 1 + nq, s);  // [0, nq): survivors; [nq]: overflow count; then the list
+  int* ovf = cnt.ptr + nq;
+  LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, (size_t)(nq + 1) * sizeof(int), s));
+  DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
+  launch_filter_scan(ma, mb, plan, nq, I.n, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
+
+  // 3. top-CT of the survivors
+  DevBuf<uint64_t> best((size_t)nq * CT, s);
+  launch_cand_select(cnt.ptr, cand.ptr, nq, plan.cap, CT, best.ptr, ovf, s);
+
+  // 4. overflow fallback (a query can only overflow when it has more survivors than slots)
+  if ((int64_t)plan.cap < I.n) {
+    ProfScope _ps("tc_fallback", s);
+    const int G = num_sms();
+    DevBuf<uint16_t> qg((size_t)qpad * KD, s);
+    launch_gather_rows(qbf.ptr, ovf, nq, qg.ptr, s);
+    const CUtensorMap mg = make_map(qg.ptr, qpad);
+    DevBuf<uint64_t> part((size_t)BM * (G + 2 * QT) * CT, s);
+    if (CT == 64) run_list_kernel<3, 64>(mg, mb, ovf, I.n, NT, G, part.ptr, I.qerr.ptr, s);
+    else run_list_kernel<1, 128>(mg, mb, ovf, I.n, NT, G, part.ptr, I.qerr.ptr, s);
+    launch_merge_fallback(part.ptr, ovf, nq, NT, G, CT, best.ptr, s);
+  }
+
+  // 5. exact FP32 re-rank with the reference's angular formula
   DevBuf<float> qn((size_t)nq, s);
   launch_row_norms(q, nq, I.d, qn.ptr, s);
-  launch_rerank(cand.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s);
+  launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s);
 }
 
 }  // namespace lshg

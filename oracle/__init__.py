@@ -204,3 +204,85 @@ def goldstandard(x, q, k, threads=1):
     ds = np.empty((q.shape[0], k), np.float32)
     t = lib().or_goldstandard(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1], k, threads, _p(ids), _p(ds))
     return ids, ds, t
+
+
+# ---- the reference's own GPU kernels (oracle/ref_harness.cpp + oracle/_ref cubins) -----
+
+REF_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_ref")
+_RH = None
+
+
+def reference_gpu_available() -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "ref_kernels.txt"))
+
+
+def ref_gpu():
+    """Load the harness and the reference cubins (GPU machine only)."""
+    global _RH
+    if _RH is None:
+        path = _build.harness_path()
+        if not os.path.exists(path):
+            _build.build_harness()
+        L = C.CDLL(path)
+        L.rh_error.restype = C.c_char_p
+        for n in ("rh_init", "rh_knn", "rh_simhash", "rh_jl", "rh_crosspoly", "rh_wmh"):
+            getattr(L, n).restype = C.c_int
+        L.rh_init.argtypes = [C.c_char_p]
+        L.rh_knn.argtypes = [P, i32, P, i32, i32, i32, i32, P, P, P]
+        L.rh_simhash.argtypes = [P, i32, i32, i32, P, i32, P]
+        L.rh_jl.argtypes = [P, i32, i32, i32, P, i32, P]
+        L.rh_crosspoly.argtypes = [P, i32, i32, i32, i32, i32, P, P]
+        L.rh_wmh.argtypes = [P, i32, i32, i32, P, P, i32, i32, i32, i32, i32, P, i32, P]
+        if L.rh_init(REF_DIR.encode()) != 0:
+            raise RuntimeError("reference harness: " + L.rh_error().decode())
+        _RH = L
+    return _RH
+
+
+def _rh_check(st):
+    if st != 0:
+        raise RuntimeError("reference harness: " + ref_gpu().rh_error().decode())
+
+
+def ref_knn(x, q, k, func=1):
+    """The reference's exact scan kernel (impl 2) -> (ids, dists, kernel ms)."""
+    x, q = _f32(x), _f32(q)
+    ids = np.empty((q.shape[0], k), np.int32)
+    ds = np.empty((q.shape[0], k), np.float32)
+    ms = C.c_float()
+    _rh_check(ref_gpu().rh_knn(_p(x), x.shape[0], _p(q), q.shape[0], x.shape[1], k, func, _p(ids), _p(ds),
+                               C.byref(ms)))
+    return ids, ds, ms.value
+
+
+def ref_simhash(x, planes, words, launch_q=64):
+    x, planes = _f32(x), _f32(planes)
+    out = np.empty((x.shape[0], words), np.uint32)
+    _rh_check(ref_gpu().rh_simhash(_p(x), x.shape[0], launch_q, x.shape[1], _p(planes), words, _p(out)))
+    return out
+
+
+def ref_jl(x, R, sdim, launch_q=64):
+    x, R = _f32(x), _f32(R)
+    out = np.empty((x.shape[0], sdim), np.float32)
+    _rh_check(ref_gpu().rh_jl(_p(x), x.shape[0], launch_q, x.shape[1], _p(R), sdim, _p(out)))
+    return out
+
+
+def ref_crosspoly(x, P_, tables, diag, launch_q=64):
+    x = _f32(x)
+    diag = np.ascontiguousarray(diag, np.int32)
+    out = np.empty((x.shape[0], tables), np.uint16)
+    _rh_check(ref_gpu().rh_crosspoly(_p(x), x.shape[0], launch_q, x.shape[1], P_, tables, _p(diag), _p(out)))
+    return out
+
+
+def ref_wmh(x, start, mp, M, H, onebit, words, hashBits, bitmap, launch_q=64):
+    x = _f32(x)
+    start = np.ascontiguousarray(start, np.int32)
+    mp = np.ascontiguousarray(mp, np.int32)
+    bitmap = np.ascontiguousarray(bitmap, np.uint8)
+    out = np.empty((x.shape[0], words), np.uint32) if onebit else np.empty((x.shape[0], H), np.uint8)
+    _rh_check(ref_gpu().rh_wmh(_p(x), x.shape[0], launch_q, x.shape[1], _p(start), _p(mp), M, H, int(onebit), words,
+                               hashBits, _p(bitmap), len(bitmap), _p(out)))
+    return out

@@ -11,6 +11,7 @@ copied into this repository.  Outputs of the reference build go to oracle/_ref o
 from __future__ import annotations
 
 import os
+import shutil
 import subprocess
 import sys
 
@@ -64,10 +65,87 @@ def build_reference() -> list[str]:
     return outs
 
 
+# Reference kernels driven by oracle/ref_harness.cpp: (tag, translation unit, demangled signature)
+REF_KERNELS = [
+    ("knn", "memOptimizedLinearScan.cu", "knn(float*, float*, int, int, int, int, Point*, int)"),
+    ("simhash_sketch", "simHash.cu", "simHash::sketch(float*, float*, int, int, int, unsigned int*)"),
+    ("crosspoly", "kernel.cu", "void crosspoly::generateHashCrossPoly<float, unsigned short>(LaunchDTO<float>, "
+                               "float*, unsigned short*, int, int, int*, float*, float*, int)"),
+    ("wmh_byte", "kernel.cu", "void weightedMinHash::sketchDataOriginal<unsigned char, unsigned char>("
+                              "LaunchDTO<unsigned char>, float*, int, int, int*, int*, int, int*, unsigned char*)"),
+    ("wmh_onebit", "kernel.cu", "void weightedMinHash::sketchDataOneBit<unsigned int, unsigned int>("
+                                "LaunchDTO<unsigned int>, float*, int, int, int, int*, int*, int, int*, bool*, "
+                                "unsigned int*)"),
+    ("jl_sketch", "kernel.cu", "void simHashJl::sketch<float>(LaunchDTO<float>, float*, float*, int, float*)"),
+]
+
+
+def build_reference_gpu() -> list[str]:
+    """Compile the reference's GPU translation units, unmodified, to sm_103a cubins in
+    oracle/_ref/ (device code only; nothing of the reference is copied), and record the
+    mangled names of the kernels the harness drives (read from the symbol table of host
+    objects compiled from the same sources)."""
+    if not reference_available():
+        return []
+    os.makedirs(REF_OUT, exist_ok=True)
+    if os.path.exists(os.path.join(REF_OUT, "ref_kernels.txt")) and not os.environ.get("LSHG_REBUILD_REF"):
+        return [os.path.join(REF_OUT, f) for f in os.listdir(REF_OUT) if f.endswith(".cubin")]
+    ls = os.path.join(REFERENCE, "LinearScan")
+    nvcc = os.environ.get("NVCC", "nvcc")
+    # template kernels keep external linkage so the harness can look them up by name
+    flags = ["-std=c++17", "-O3", "-include", "cuda.h", "-I" + ls, "-w", "-static-global-template-stub=false"]
+    outs = []
+    names = {}
+    for tu in sorted({k[1] for k in REF_KERNELS}):
+        stem = os.path.splitext(tu)[0]
+        cubin = os.path.join(REF_OUT, f"ref_{stem}.cubin")
+        _run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", *flags, os.path.join(ls, tu), "-o", cubin])
+        outs.append(cubin)
+        obj = os.path.join(REF_OUT, f"host_{stem}.o")
+        _run([nvcc, "-c", "-gencode", "arch=compute_103a,code=sm_103a", *flags, os.path.join(ls, tu), "-o", obj])
+        syms = subprocess.run(["nm", "--defined-only", obj], capture_output=True, text=True, check=True).stdout
+        mangled = [line.split()[-1] for line in syms.splitlines() if len(line.split()) >= 3]
+        dem = subprocess.run(["c++filt"], input="\n".join(mangled), capture_output=True, text=True,
+                             check=True).stdout.splitlines()
+        for tag, unit, sig in REF_KERNELS:
+            if unit != tu:
+                continue
+            for m, d in zip(mangled, dem):
+                if d == sig:
+                    names[tag] = (f"ref_{stem}.cubin", m)
+        os.remove(obj)
+    missing = [t for t, _, _ in REF_KERNELS if t not in names]
+    if missing:
+        raise RuntimeError("reference kernels not found in the symbol tables: " + ", ".join(missing))
+    with open(os.path.join(REF_OUT, "ref_kernels.txt"), "w") as f:
+        for tag, (cubin, m) in sorted(names.items()):
+            f.write(f"{tag} {cubin} {m}\n")
+    return outs
+
+
+def harness_path() -> str:
+    return os.path.join(BUILD, "libref_harness.so")
+
+
+def build_harness() -> str:
+    """The driver-API harness that runs the reference cubins (needs only the CUDA
+    toolkit; the cubins come prebuilt from oracle/_ref)."""
+    os.makedirs(BUILD, exist_ok=True)
+    out = harness_path()
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    stubs = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64", "stubs")
+    _run([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-o", out + ".tmp",
+          os.path.join(HERE, "ref_harness.cpp"), "-L" + stubs, "-lcuda"])
+    os.replace(out + ".tmp", out)
+    return out
+
+
 def build(with_reference: bool = True) -> str:
     out = build_oracle()
+    build_harness()
     if with_reference:
         build_reference()
+        build_reference_gpu()
     return out
 
 

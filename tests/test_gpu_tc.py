@@ -58,3 +58,57 @@ def test_tc_rejects_unsupported(engine):
         idx.query(x[:4], 256)
     with pytest.raises(engine.LshgError):
         engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=2)
+
+
+def _query_both_paths(idx, q, k):
+    """The filter path and the per-row list kernel (forced for every query) on the same
+    inputs."""
+    import os
+
+    a = idx.query(q, k)
+    os.environ["LSHG_TC_FORCE_FALLBACK"] = "1"
+    try:
+        b = idx.query(q, k)
+    finally:
+        del os.environ["LSHG_TC_FORCE_FALLBACK"]
+    return a, b
+
+
+# n chosen to exercise every prepass regime: no prepass (keep every point), 8-column
+# group maxima, 64-column maxima of every tile, and of every second tile
+@pytest.mark.parametrize("n,nq,k", [(1500, 64, 32), (6000, 129, 32), (20000, 200, 32), (140000, 256, 32),
+                                    (40000, 130, 100)])
+def test_tc_filter_path_equals_list_kernel(engine, orc, n, nq, k):
+    x = datasets.clustered(n, D, 81, count=60)
+    q = datasets.clustered(nq, D, 82, count=60)
+    idx = engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=1)
+    a, b = _query_both_paths(idx, q, k)
+    # both select the exact top-CT by tensor-core score, so the outputs are identical
+    assert np.array_equal(a["ID"], b["ID"])
+    assert np.array_equal(a["distance"], b["distance"])
+    sub = min(nq, 40)
+    ids, _ = orc.exact_topk(x, q[:sub], k, dist=1)
+    assert recall(a["ID"][:sub], ids) >= 0.99
+
+
+def test_tc_overflow_duplicates(engine, orc):
+    """5,000 copies of one point: a query at that point has 5,000 tied survivors, more than
+    its candidate array holds, and goes through the on-device list-kernel fallback; the
+    other queries of the same batch stay on the filter path."""
+    n = 20000
+    x = datasets.clustered(n, D, 91, count=40)
+    x[1000:6000] = x[777]
+    q = datasets.clustered(48, D, 92, count=40)
+    q[5] = x[777]
+    q[17] = x[777] * 3.0   # same direction
+    q[30] = x[777] + 0.001 * q[30]
+    idx = engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=1)
+    res = idx.query(q, 32)
+    ids, ds = orc.exact_topk(x, q, 32, dist=1)
+    for i in (5, 17):
+        # ties broken by the lower id: the point itself, then the first copies
+        assert res["ID"][i].tolist() == ids[i].tolist()
+        assert np.array_equal(res["distance"][i], ds[i])
+    assert recall(res["ID"], ids) >= 0.99
+    a, b = _query_both_paths(idx, q, 32)
+    assert np.array_equal(a["ID"], b["ID"]) and np.array_equal(a["distance"], b["distance"])
