@@ -49,10 +49,14 @@ constexpr int F_NACC = 4;
 constexpr int F_TMEM_COLS = F_NACC * BN;
 constexpr int F_EPI_WARPS = 8;
 
+constexpr int F_SBUF = 16;  // staged survivors a row and warpgroup (flushed with one atomic)
+
 constexpr int F_A_OFF = 0;                               // two query tiles
 constexpr int F_B_OFF = 2 * TILE_BYTES;                  // F_STAGES base tiles
-constexpr int F_BAR_OFF = F_B_OFF + F_STAGES * TILE_BYTES;
+constexpr int F_S_OFF = F_B_OFF + F_STAGES * TILE_BYTES;  // survivor staging: scores then ids, [2][F_SBUF][BM]
+constexpr int F_BAR_OFF = F_S_OFF + 2 * F_SBUF * BM * 8;
 constexpr int F_SMEM = F_BAR_OFF + 256 + 1024;           // + barriers + 1 KB alignment slack
+static_assert(F_SMEM <= 232448, "shared memory per CTA");
 
 struct FilterArgs {
   int nq;
@@ -68,6 +72,7 @@ struct FilterArgs {
   int* cnt;          // survivors per query
   uint64_t* cand;    // [nq][cap] survivor keys
   int cap;
+  int ksteps;    // K=16 MMA steps covering the data dimension
   int* err;
 };
 
@@ -168,7 +173,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           const int st = it % F_STAGES, rd = it / F_STAGES;
           if (!mbar_wait(FULL(st), rd & 1, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          umma_tile(tmem + (uint32_t)(b * BN), s0 + F_A_OFF + ab * TILE_BYTES, s0 + F_B_OFF + st * TILE_BYTES);
+          umma_tile(tmem + (uint32_t)(b * BN), s0 + F_A_OFF + ab * TILE_BYTES, s0 + F_B_OFF + st * TILE_BYTES,
+                    a.ksteps);
           umma_commit(EMPTY(st));
           umma_commit(ACC_FULL(b));
           ++it;
@@ -185,12 +191,28 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const int g = (warp - 4) >> 2;               // column half of every accumulator
     const int r = (warp & 3) * 32 + lane;        // query row within the tile = TMEM lane
     const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(g * 64);
+    // Survivors are staged per row in shared memory as (score, id) -- this thread's own
+    // column of the warpgroup's [F_SBUF][BM] arrays, so no synchronisation is needed --
+    // and reach the query's global array in batches: one atomicAdd a flush instead of
+    // one a survivor, and the ordering keys are built only then.
+    float* ssc = reinterpret_cast<float*>(sm + F_S_OFF) + (size_t)g * F_SBUF * BM + r;
+    int* sid = reinterpret_cast<int*>(sm + F_S_OFF + 2 * F_SBUF * BM * 4) + (size_t)g * F_SBUF * BM + r;
+    int scnt = 0;
     int it = 0;
     bool ok = true;
     for (int u = blockIdx.x; u < U && ok; u += gridDim.x) {
       const int qt = u % a.QT, c = u / a.QT;
       const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
       const int q = qt * BM + r;
+      auto flush = [&]() {
+        if (scnt > 0) {
+          const int base = atomicAdd(a.cnt + q, scnt);
+          uint64_t* dst = a.cand + (int64_t)q * a.cap;
+          for (int e = 0; e < scnt; ++e)
+            if (base + e < a.cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
+          scnt = 0;
+        }
+      };
       float tau = INFINITY;
       if (MODE == MODE_FILTER && q < a.nq) tau = a.tau ? a.tau[q] : -INFINITY;
       for (int p = p0; p < p1; ++p) {
@@ -228,27 +250,35 @@ __global__ void __launch_bounds__(F_THREADS, 1)
             }
           }
         } else {
+          if (cbase + 64 > a.n) {  // last base tile: padding rows become NaN, which never passes
+#pragma unroll
+            for (int j = 0; j < 64; ++j)
+              if (cbase + j >= a.n) v[j] = 0x7fc00000u;
+          }
           float m[8];
 #pragma unroll
           for (int gg = 0; gg < 8; ++gg) m[gg] = max8(v, gg);
           const float tm = max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]), fmaxf(m[6], m[7]));
           if (__any_sync(0xffffffffu, tm >= tau)) {
+            const int ibase = (int)cbase;  // ids fit in 32 bits (n < 2^31)
 #pragma unroll
             for (int gg = 0; gg < 8; ++gg) {
               if (!__any_sync(0xffffffffu, m[gg] >= tau)) continue;
 #pragma unroll
               for (int jj = 0; jj < 8; ++jj) {
                 const float s = __uint_as_float(v[8 * gg + jj]);
-                const int64_t pid = cbase + 8 * gg + jj;
-                if (s >= tau && pid < a.n) {
-                  const int slot = atomicAdd(a.cnt + q, 1);
-                  if (slot < a.cap) a.cand[(int64_t)q * a.cap + slot] = make_key(-s, (int)pid);
+                if (s >= tau) {
+                  ssc[scnt * BM] = s;
+                  sid[scnt * BM] = ibase + 8 * gg + jj;
+                  ++scnt;
                 }
               }
+              if (__any_sync(0xffffffffu, scnt > F_SBUF - 8)) flush();  // the next group adds <= 8
             }
           }
         }
       }
+      if (MODE == MODE_FILTER) flush();  // the next unit is another query tile
     }
   }
 
@@ -439,9 +469,10 @@ FilterPlan plan_filter(int64_t n, int CT) {
 }
 
 void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const FilterPlan& plan, int nq, int64_t n,
-                        int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s) {
+                        int d, int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s) {
   FilterArgs a{};
   a.nq = nq;
+  a.ksteps = tc_ksteps(d);
   a.n = n;
   a.QT = QT;
   a.err = err;

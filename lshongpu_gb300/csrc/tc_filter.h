@@ -30,7 +30,7 @@ FilterPlan plan_filter(int64_t n, int CT);
 
 // Prepass + threshold selection + filter pass: fills cnt[q] and cand[q][0..cap).
 void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const FilterPlan& plan, int nq, int64_t n,
-                        int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s);
+                        int d, int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s);
 
 // Top-CT keys a query from its survivors; overflowed queries are listed in ovf.
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,

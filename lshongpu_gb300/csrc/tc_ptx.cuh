@@ -92,14 +92,19 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t 
       "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
       : "memory");
 }
-// One 128 x 128 x 128 product: eight K=16 steps over the two 64-column swizzled halves.
-__device__ __forceinline__ void umma_tile(uint32_t d_tmem, uint32_t a_base, uint32_t b_base) {
+// One 128 x 128 x (16 * ksteps) product: K=16 steps over the two 64-column swizzled
+// halves.  Rows are zero beyond the data dimension d, so ksteps = ceil(d / 16) gives the
+// same FP32 sums as all eight steps (the skipped steps would add exact zeros).
+__device__ __forceinline__ void umma_tile(uint32_t d_tmem, uint32_t a_base, uint32_t b_base, int ksteps) {
 #pragma unroll
   for (int kk = 0; kk < KD / 16; ++kk) {
-    const uint32_t off = (kk >> 2) * HALF_BYTES + (kk & 3) * 32;
-    umma_bf16(d_tmem, smem_desc(a_base + off), smem_desc(b_base + off), kk > 0 ? 1u : 0u);
+    if (kk < ksteps) {
+      const uint32_t off = (kk >> 2) * HALF_BYTES + (kk & 3) * 32;
+      umma_bf16(d_tmem, smem_desc(a_base + off), smem_desc(b_base + off), kk > 0 ? 1u : 0u);
+    }
   }
 }
+__host__ __device__ inline int tc_ksteps(int d) { return d <= 0 ? 1 : (d > KD ? KD / 16 : (d + 15) / 16); }
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }

@@ -146,7 +146,8 @@ __device__ __noinline__ float warp_fold_row(float* lsc, int* lid, const float* b
 template <int STAGES, int CT>
 __global__ void __launch_bounds__(NTHREADS, 1)
     tc_list_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                   const int* __restrict__ rows_dev, int64_t n, int NT, uint64_t* __restrict__ part, int* err) {
+                   const int* __restrict__ rows_dev, int64_t n, int NT, int ksteps, uint64_t* __restrict__ part,
+                   int* err) {
   constexpr TcLayout L = tc_layout(STAGES, CT);
   constexpr int fold_limit = BUFN - 8;
   const int nq = *rows_dev;  // gathered query rows (0: nothing to do)
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int st = it % STAGES, rd = it / STAGES;
         if (!mbar_wait(FULL(st), rd & 1, abort_flag)) break;
         tc_fence_after();
-        umma_tile(tmem + (uint32_t)(b * BN), s0 + L.a_off, s0 + L.b_off + st * TILE_BYTES);
+        umma_tile(tmem + (uint32_t)(b * BN), s0 + L.a_off, s0 + L.b_off + st * TILE_BYTES, ksteps);
         umma_commit(EMPTY(st));
         umma_commit(ACC_FULL(b));
         const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
@@ -429,12 +430,12 @@ CUtensorMap make_map(const void* base, int64_t rows) {
 namespace {
 
 template <int STAGES, int CT>
-void run_list_kernel(const CUtensorMap& ma, const CUtensorMap& mb, const int* rows_dev, int64_t n, int NT, int grid,
-                     uint64_t* part, int* err, cudaStream_t s) {
+void run_list_kernel(const CUtensorMap& ma, const CUtensorMap& mb, const int* rows_dev, int64_t n, int NT, int d,
+                     int grid, uint64_t* part, int* err, cudaStream_t s) {
   constexpr TcLayout L = tc_layout(STAGES, CT);
   auto kern = tc_list_kernel<STAGES, CT>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total));
-  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, rows_dev, n, NT, part, err);
+  kern<<<grid, NTHREADS, L.total, s>>>(ma, mb, rows_dev, n, NT, tc_ksteps(d), part, err);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
@@ -476,7 +477,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   int* ovf = cnt.ptr + nq;
   LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, (size_t)(nq + 1) * sizeof(int), s));
   DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
-  launch_filter_scan(ma, mb, plan, nq, I.n, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
+  launch_filter_scan(ma, mb, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
 
   // 3. top-CT of the survivors
   DevBuf<uint64_t> best((size_t)nq * CT, s);
@@ -490,8 +491,8 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
     launch_gather_rows(qbf.ptr, ovf, nq, qg.ptr, s);
     const CUtensorMap mg = make_map(qg.ptr, qpad);
     DevBuf<uint64_t> part((size_t)BM * (G + 2 * QT) * CT, s);
-    if (CT == 64) run_list_kernel<3, 64>(mg, mb, ovf, I.n, NT, G, part.ptr, I.qerr.ptr, s);
-    else run_list_kernel<1, 128>(mg, mb, ovf, I.n, NT, G, part.ptr, I.qerr.ptr, s);
+    if (CT == 64) run_list_kernel<3, 64>(mg, mb, ovf, I.n, NT, I.d, G, part.ptr, I.qerr.ptr, s);
+    else run_list_kernel<1, 128>(mg, mb, ovf, I.n, NT, I.d, G, part.ptr, I.qerr.ptr, s);
     launch_merge_fallback(part.ptr, ovf, nq, NT, G, CT, best.ptr, s);
   }
 
