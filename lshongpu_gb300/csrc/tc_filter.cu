@@ -25,10 +25,11 @@
 // query tiles, so each base tile is read from HBM about once and served from L2 to the
 // other query tiles; the query tile of a unit is double-buffered in shared memory.
 //
-// Warp roles (384 threads): warp 0 TMA producer, warp 1 MMA issuer (one elected thread),
-// warp 2 TMEM allocator (4 accumulators x 128 columns = 512), warp 3 idle, warps 4-11 the
-// epilogue: warpgroup g (warps 4+4g .. 7+4g) reads TMEM columns [64g, 64g+64) of every
-// accumulator, thread (warp & 3) * 32 + lane owns query row = TMEM lane.  Every mbarrier
+// Tiles are 128 queries x 256 base points (tcgen05.mma M = 128, N = 256).  Warp roles (640
+// threads): warp 0 TMA producer, warp 1 MMA issuer (one elected thread), warp 2 TMEM
+// allocator (2 accumulators x 256 columns = 512), warp 3 idle, warps 4-19 the epilogue:
+// warpgroup g (warps 4+4g .. 7+4g) reads TMEM columns [64g, 64g+64) of every accumulator,
+// thread (warp & 3) * 32 + lane owns query row = TMEM lane.  Every mbarrier
 // wait is bounded; a CTA that times out raises the error flag, drains its own copies and
 // MMAs, frees TMEM and returns.
 #include "index.h"
@@ -43,19 +44,22 @@ namespace tc {
 
 namespace {
 
-constexpr int F_THREADS = 384;
-constexpr int F_STAGES = 4;
-constexpr int F_NACC = 4;
-constexpr int F_TMEM_COLS = F_NACC * BN;
-constexpr int F_EPI_WARPS = 8;
+constexpr int F_THREADS = 640;
+constexpr int TN = FILTER_TN;                   // base points a tile = UMMA N
+constexpr int B_HALF = TN * KHALF * 2;          // 32 KB: one 64-column half of a base tile
+constexpr int B_TILE = 2 * B_HALF;              // 64 KB
+constexpr int F_STAGES = 2;
+constexpr int F_NACC = 2;                       // TMEM accumulators of TN columns
+constexpr int F_TMEM_COLS = F_NACC * TN;        // 512 = all of TMEM (one CTA per SM)
+constexpr int F_EPI_WARPS = 16;  // four warpgroups, one 64-column piece each
 
-constexpr int F_SBUF = 16;  // staged survivors a row and warpgroup (flushed with one atomic)
+constexpr int F_SBUF = 8;  // staged survivors a row and warpgroup (flushed with one atomic)
 
-constexpr int F_A_OFF = 0;                               // two query tiles
-constexpr int F_B_OFF = 2 * TILE_BYTES;                  // F_STAGES base tiles
-constexpr int F_S_OFF = F_B_OFF + F_STAGES * TILE_BYTES;  // survivor staging: scores then ids, [2][F_SBUF][BM]
-constexpr int F_BAR_OFF = F_S_OFF + 2 * F_SBUF * BM * 8;
-constexpr int F_SMEM = F_BAR_OFF + 256 + 1024;           // + barriers + 1 KB alignment slack
+constexpr int F_A_OFF = 0;                                // two query tiles
+constexpr int F_B_OFF = 2 * TILE_BYTES;                   // F_STAGES base tiles
+constexpr int F_S_OFF = F_B_OFF + F_STAGES * B_TILE;      // survivor staging: scores then ids, [4][F_SBUF][BM]
+constexpr int F_BAR_OFF = F_S_OFF + 4 * F_SBUF * BM * 8;
+constexpr int F_SMEM = F_BAR_OFF + 256 + 1024;            // + barriers + 1 KB alignment slack
 static_assert(F_SMEM <= 232448, "shared memory per CTA");
 
 struct FilterArgs {
@@ -80,7 +84,7 @@ template <int MODE, int GW>
 __global__ void __launch_bounds__(F_THREADS, 1)
     tc_filter_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                      const FilterArgs a) {
-  static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column halves");
+  static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column pieces");
   static_assert(GW == 64 || GW == 8, "group width");
   const int U = a.NCH * a.QT;
   if ((int)blockIdx.x >= U) return;  // no unit for this CTA: leave before any barrier or TMEM use
@@ -141,11 +145,11 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         for (int p = p0; p < p1; ++p) {
           const int st = it % F_STAGES, rd = it / F_STAGES;
           if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
-          const uint32_t dst = s0 + F_B_OFF + st * TILE_BYTES;
-          const int row = p * a.dstride * BN;
-          mbar_expect_tx(FULL(st), TILE_BYTES);
+          const uint32_t dst = s0 + F_B_OFF + st * B_TILE;
+          const int row = p * a.dstride * TN;
+          mbar_expect_tx(FULL(st), B_TILE);
           tma_load_2d(dst, &mapB, 0, row, FULL(st));
-          tma_load_2d(dst + HALF_BYTES, &mapB, KHALF, row, FULL(st));
+          tma_load_2d(dst + B_HALF, &mapB, KHALF, row, FULL(st));
           ++it;
         }
       }
@@ -173,8 +177,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           const int st = it % F_STAGES, rd = it / F_STAGES;
           if (!mbar_wait(FULL(st), rd & 1, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          umma_tile(tmem + (uint32_t)(b * BN), s0 + F_A_OFF + ab * TILE_BYTES, s0 + F_B_OFF + st * TILE_BYTES,
-                    a.ksteps);
+          umma_tile<TN>(tmem + (uint32_t)(b * TN), s0 + F_A_OFF + ab * TILE_BYTES, s0 + F_B_OFF + st * B_TILE,
+                        a.ksteps);
           umma_commit(EMPTY(st));
           umma_commit(ACC_FULL(b));
           ++it;
@@ -188,7 +192,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     __syncwarp();
   } else if (warp >= 4) {
     // ---------------- epilogue ----------------
-    const int g = (warp - 4) >> 2;               // column half of every accumulator
+    const int g = (warp - 4) >> 2;               // warpgroup: columns [64g, 64g+64) of every accumulator
     const int r = (warp & 3) * 32 + lane;        // query row within the tile = TMEM lane
     const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(g * 64);
     // Survivors are staged per row in shared memory as (score, id) -- this thread's own
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     // and reach the query's global array in batches: one atomicAdd a flush instead of
     // one a survivor, and the ordering keys are built only then.
     float* ssc = reinterpret_cast<float*>(sm + F_S_OFF) + (size_t)g * F_SBUF * BM + r;
-    int* sid = reinterpret_cast<int*>(sm + F_S_OFF + 2 * F_SBUF * BM * 4) + (size_t)g * F_SBUF * BM + r;
+    int* sid = reinterpret_cast<int*>(sm + F_S_OFF + 4 * F_SBUF * BM * 4) + (size_t)g * F_SBUF * BM + r;
     int scnt = 0;
     int it = 0;
     bool ok = true;
@@ -220,13 +224,14 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         if (!mbar_wait(ACC_FULL(b), ub & 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
         uint32_t v[64];
-        tmem_ld64(tbase + (uint32_t)(b * BN), v);
+        tmem_ld64(tbase + (uint32_t)(b * TN), v);
         tmem_wait_ld();
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(ACC_EMPTY(b));  // scores are in registers: the MMA may reuse the buffer
         ++it;
-        const int64_t cbase = (int64_t)p * a.dstride * BN + g * 64;  // base id of v[0]
+        const int64_t cbase = (int64_t)p * a.dstride * TN + g * 64;  // base id of v[0]
+        const int piece = 4 * p + g;  // index of this 64-column piece among the row's sampled pieces
         if (MODE == MODE_GROUPMAX) {
           if (cbase + 64 > a.n) {  // last base tile: padding rows are not points
 #pragma unroll
@@ -238,13 +243,13 @@ __global__ void __launch_bounds__(F_THREADS, 1)
               float m[8];
 #pragma unroll
               for (int gg = 0; gg < 8; ++gg) m[gg] = max8(v, gg);
-              a.gmax[(int64_t)q * a.M + 2 * p + g] =
+              a.gmax[(int64_t)q * a.M + piece] =
                   max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]), fmaxf(m[6], m[7]));
             } else {
               float4 lo, hi;
               lo.x = max8(v, 0); lo.y = max8(v, 1); lo.z = max8(v, 2); lo.w = max8(v, 3);
               hi.x = max8(v, 4); hi.y = max8(v, 5); hi.z = max8(v, 6); hi.w = max8(v, 7);
-              float4* dst = reinterpret_cast<float4*>(a.gmax + (int64_t)q * a.M + 16 * p + 8 * g);
+              float4* dst = reinterpret_cast<float4*>(a.gmax + (int64_t)q * a.M + 8 * piece);
               dst[0] = lo;
               dst[1] = hi;
             }
@@ -264,6 +269,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
 #pragma unroll
             for (int gg = 0; gg < 8; ++gg) {
               if (!__any_sync(0xffffffffu, m[gg] >= tau)) continue;
+              if (m[gg] >= tau && scnt > F_SBUF - 8) flush();  // this group may add 8
 #pragma unroll
               for (int jj = 0; jj < 8; ++jj) {
                 const float s = __uint_as_float(v[8 * gg + jj]);
@@ -273,7 +279,6 @@ __global__ void __launch_bounds__(F_THREADS, 1)
                   ++scnt;
                 }
               }
-              if (__any_sync(0xffffffffu, scnt > F_SBUF - 8)) flush();  // the next group adds <= 8
             }
           }
         }
@@ -354,24 +359,81 @@ __global__ void __launch_bounds__(256) tau_select_kernel(const float* __restrict
   if (lane == 0) tau[q] = ordered_to_float(prefix) - margin;
 }
 
-// Per query: sort the survivors and keep the first CT keys; list queries whose survivors
-// overflowed the candidate array (ovf[0] = count, ovf[1..] = query ids).
-__global__ void cand_select_kernel(const int* __restrict__ cnt, const uint64_t* __restrict__ cand, int cap, int CT,
-                                   uint64_t* __restrict__ out, int* __restrict__ ovf) {
-  extern __shared__ uint64_t ks[];
-  const int q = blockIdx.x;
+// Warp-wide bitonic network on 32*E 64-bit keys held as x[e] of lane l = element e*32+l.
+// Sorts ascending when `merge_only` is false; with `merge_only` the input must already
+// be bitonic and one merge pass sorts it.
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint64_t (&x)[E], int lane, bool merge_only) {
+  constexpr int N = 32 * E;
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1) {
+    if (merge_only && k != N) continue;
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int i = e * 32 + lane;
+        const bool up = (i & k) == 0 || merge_only;
+        if (j >= 32) {
+          const int f = e ^ (j >> 5);
+          if (f > e) {  // both elements live in this lane
+            const uint64_t lo = x[e] < x[f] ? x[e] : x[f];
+            const uint64_t hi = x[e] < x[f] ? x[f] : x[e];
+            x[e] = up ? lo : hi;
+            x[f] = up ? hi : lo;
+          }
+        } else {
+          const uint64_t o = __shfl_xor_sync(0xffffffffu, x[e], j);
+          const bool lower = (lane & j) == 0;
+          x[e] = (lower == up) ? (x[e] < o ? x[e] : o) : (x[e] < o ? o : x[e]);
+        }
+      }
+    }
+  }
+}
+
+// Per query (one warp): the CT = 32*E smallest keys of the survivors -- sort each chunk of
+// CT keys and merge it into the running result with a bitonic "min + merge" step.  Lists
+// queries whose survivors overflowed the candidate array (ovf[0] = count, ovf[1..] = ids).
+template <int E>
+__global__ void __launch_bounds__(256) cand_select_kernel(const int* __restrict__ cnt,
+                                                           const uint64_t* __restrict__ cand, int cap, int nq,
+                                                           uint64_t* __restrict__ out, int* __restrict__ ovf) {
+  constexpr int CT = 32 * E;
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (q >= nq) return;  // warp-uniform
   const int c = cnt[q];
+  uint64_t* dst = out + (int64_t)q * CT;
   if (c > cap) {
-    for (int i = threadIdx.x; i < CT; i += blockDim.x) out[(int64_t)q * CT + i] = kEmptyKey;
-    if (threadIdx.x == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
+#pragma unroll
+    for (int e = 0; e < E; ++e) dst[e * 32 + lane] = kEmptyKey;
+    if (lane == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
     return;
   }
-  int P = CT;
-  while (P < c) P <<= 1;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) ks[i] = i < c ? cand[(int64_t)q * cap + i] : kEmptyKey;
-  __syncthreads();
-  block_bitonic_sort(ks, P);
-  for (int i = threadIdx.x; i < CT; i += blockDim.x) out[(int64_t)q * CT + i] = ks[i];
+  const uint64_t* src = cand + (int64_t)q * cap;
+  uint64_t best[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) best[e] = kEmptyKey;
+  for (int base = 0; base < c; base += CT) {
+    uint64_t x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int i = base + e * 32 + lane;
+      x[e] = i < c ? src[i] : kEmptyKey;
+    }
+    warp_bitonic<E>(x, lane, false);
+    // best ascending, x ascending: min(best[i], x[CT-1-i]) is bitonic and holds the CT
+    // smallest of the union
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const uint64_t r = __shfl_sync(0xffffffffu, x[E - 1 - e], 31 - lane);
+      best[e] = best[e] < r ? best[e] : r;
+    }
+    warp_bitonic<E>(best, lane, true);
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) dst[e * 32 + lane] = best[e];
 }
 
 // Compact the bf16 rows of the listed queries into rows 0..count-1 of `dst` (the rest of
@@ -441,30 +503,33 @@ void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, FilterArgs a, cons
 
 }  // namespace
 
+// Prepass parameters in units of TN-point tiles.  The target is M (group maxima a row)
+// of at least 4 CT, so that the CT-th largest maximum is a tight bound, and a sample of
+// at most 1/8 of the base; survivors then number about CT * S a query.
 FilterPlan plan_filter(int64_t n, int CT) {
   FilterPlan p{};
-  const int NT = ceil_div(n, BN);
+  const int NT = ceil_div(n, TN);
   p.NT = NT;
-  if (NT >= 2 * CT) {
+  if (NT >= CT) {  // 64-column maxima: 4 a tile
     p.GW = 64;
-    p.S = (int)std::max<int64_t>(1, std::min<int64_t>(8, NT / (8 * CT)));
+    p.S = (int)std::max<int64_t>(1, std::min<int64_t>(8, NT / (4 * CT)));
     p.NS = ceil_div(NT, p.S);
-    p.M = 2 * p.NS;
+    p.M = 4 * p.NS;
     p.cap = std::max(1024, 4 * CT * p.S);
-  } else if (NT * 16 >= 4 * CT) {
+  } else if (NT * 32 >= 4 * CT) {  // 8-column maxima: 32 a tile
     p.GW = 8;
     p.S = 1;
     p.NS = NT;
-    p.M = 16 * NT;
+    p.M = 32 * NT;
     p.cap = std::max(1024, 4 * CT);
   } else {  // a few thousand points: keep every one
     p.GW = 0;
     p.S = 1;
     p.NS = 0;
     p.M = 0;
-    p.cap = NT * BN;
+    p.cap = NT * TN;
   }
-  p.cap = std::min<int64_t>(p.cap, (int64_t)NT * BN);
+  p.cap = std::min<int64_t>(p.cap, (int64_t)NT * TN);
   return p;
 }
 
@@ -504,13 +569,10 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const Filt
 
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
                         cudaStream_t s) {
-  int P = CT;
-  while (P < cap) P <<= 1;
-  const size_t smem = (size_t)P * 8;
-  LSHG_REQUIRE(smem <= 200 * 1024, "tensor-core scan: candidate array too large");
   ProfScope _ps("tc_cand_select", s);
-  LSHG_CUDA(cudaFuncSetAttribute(cand_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  cand_select_kernel<<<nq, 256, smem, s>>>(cnt, cand, cap, CT, out, ovf);
+  if (CT == 64) cand_select_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
+  else if (CT == 128) cand_select_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
+  else throw Error(LSHG_ERR_INVALID_ARGUMENT, "tensor-core scan: candidate count must be 64 or 128");
   count_launch();
   LSHG_CHECK_LAUNCH();
 }

@@ -9,6 +9,7 @@
 namespace lshg {
 namespace tc {
 
+constexpr int FILTER_TN = 256;    // base points a filter tile (UMMA N)
 constexpr int MODE_GROUPMAX = 0;  // prepass: per-row group maxima of sampled tiles
 constexpr int MODE_FILTER = 1;    // main pass: keep scores >= the row's threshold
 
@@ -18,7 +19,7 @@ constexpr float kTauMargin = 1e-6f;
 
 // Parameters of the threshold prepass for a base of n points and CT candidates a query.
 struct FilterPlan {
-  int NT;   // base tiles
+  int NT;   // 256-point base tiles
   int GW;   // group width of the prepass maxima (64 or 8; 0 = no prepass, keep every point)
   int S;    // prepass samples every S-th base tile
   int NS;   // sampled tiles

@@ -81,26 +81,32 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
          ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major, M = 128, N = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
           tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
-// One 128 x 128 x (16 * ksteps) product: K=16 steps over the two 64-column swizzled
-// halves.  Rows are zero beyond the data dimension d, so ksteps = ceil(d / 16) gives the
-// same FP32 sums as all eight steps (the skipped steps would add exact zeros).
+// One 128 x N x (16 * ksteps) product; A is a 128-row tile and B an N-row tile, both
+// stored as two 64-column swizzled halves (A half = 16 KB, B half = N * 128 B).  Rows are
+// zero beyond the data dimension d, so ksteps = ceil(d / 16) gives the same FP32 sums as
+// all eight steps (the skipped steps would add exact zeros).
+template <int N>
 __device__ __forceinline__ void umma_tile(uint32_t d_tmem, uint32_t a_base, uint32_t b_base, int ksteps) {
+  constexpr uint32_t idesc = idesc_bf16(BM, N);
 #pragma unroll
   for (int kk = 0; kk < KD / 16; ++kk) {
     if (kk < ksteps) {
-      const uint32_t off = (kk >> 2) * HALF_BYTES + (kk & 3) * 32;
-      umma_bf16(d_tmem, smem_desc(a_base + off), smem_desc(b_base + off), kk > 0 ? 1u : 0u);
+      const uint32_t koff = (kk & 3) * 32;
+      umma_bf16(d_tmem, smem_desc(a_base + (kk >> 2) * HALF_BYTES + koff),
+                smem_desc(b_base + (kk >> 2) * (N * 128) + koff), idesc, kk > 0 ? 1u : 0u);
     }
   }
 }
@@ -153,9 +159,9 @@ __device__ __forceinline__ float max8(const uint32_t (&v)[64], int g) {
                fmaxf(__uint_as_float(v[8 * g + 6]), __uint_as_float(v[8 * g + 7])));
 }
 
-// Tensor map over `rows` bf16 rows of KD elements; boxes of 64 columns x 128 rows with
-// 128-byte swizzle (the layout smem_desc describes).
-CUtensorMap make_map(const void* base, int64_t rows);
+// Tensor map over `rows` bf16 rows of KD elements; boxes of 64 columns x box_rows rows
+// with 128-byte swizzle (the layout smem_desc describes).
+CUtensorMap make_map(const void* base, int64_t rows, int box_rows = BM);
 
 }  // namespace tc
 }  // namespace lshg

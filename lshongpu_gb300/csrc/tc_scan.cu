@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int st = it % STAGES, rd = it / STAGES;
         if (!mbar_wait(FULL(st), rd & 1, abort_flag)) break;
         tc_fence_after();
-        umma_tile(tmem + (uint32_t)(b * BN), s0 + L.a_off, s0 + L.b_off + st * TILE_BYTES, ksteps);
+        umma_tile<BN>(tmem + (uint32_t)(b * BN), s0 + L.a_off, s0 + L.b_off + st * TILE_BYTES, ksteps);
         umma_commit(EMPTY(st));
         umma_commit(ACC_FULL(b));
         const bool last_of_qt = (t + 1 == t_end) || ((t + 1) / NT != qt);
@@ -413,12 +413,13 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // Rows of KD bf16 (256 B); boxes of 64 columns x 128 rows with 128-byte swizzle.
-CUtensorMap make_map(const void* base, int64_t rows) {
+CUtensorMap make_map(const void* base, int64_t rows, int box_rows) {
   LSHG_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
   CUtensorMap m;
   cuuint64_t dims[2] = {(cuuint64_t)KD, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)KD * 2};
-  cuuint32_t box[2] = {(cuuint32_t)KHALF, (cuuint32_t)BM};
+  LSHG_REQUIRE(box_rows >= 1 && box_rows <= 256, "TMA box rows must be in [1, 256]");
+  cuuint32_t box[2] = {(cuuint32_t)KHALF, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -448,7 +449,7 @@ void tc_prepare(Index& I, cudaStream_t s) {
   LSHG_REQUIRE(I.dist == DIST_ANGULAR, "tensor-core scan: angular distance only");
   LSHG_REQUIRE(I.d <= KD, "tensor-core scan: dimension must be <= 128");
   I.dp = KD;
-  const int64_t npad = (int64_t)ceil_div(I.n, BN) * BN;
+  const int64_t npad = (int64_t)ceil_div(I.n, FILTER_TN) * FILTER_TN;  // whole filter tiles
   I.xbf.alloc((size_t)npad * KD, s);
   to_unit_bf16(I.x.ptr, I.n, I.d, npad, I.xbf.ptr, s);
 }
@@ -464,12 +465,14 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   // test hook: LSHG_TC_FORCE_FALLBACK=1 sends every query through the list kernel, so
   // tests can compare the two selection paths on the same inputs
   if (const char* e = getenv("LSHG_TC_FORCE_FALLBACK"); e && e[0] == '1') plan.cap = 0;
-  const int NT = plan.NT;
+  const int NT = ceil_div(I.n, BN);  // 128-row tiles of the list kernel
   LSHG_REQUIRE((int64_t)QT * NT < (int64_t)INT_MAX, "tensor-core scan: problem too large");
   DevBuf<uint16_t> qbf((size_t)qpad * KD, s);
   to_unit_bf16(q, nq, I.d, qpad, qbf.ptr, s);
   const CUtensorMap ma = make_map(qbf.ptr, qpad);
-  const CUtensorMap mb = make_map(I.xbf.ptr, (int64_t)NT * BN);
+  const int64_t npad = (int64_t)ceil_div(I.n, FILTER_TN) * FILTER_TN;
+  const CUtensorMap mb = make_map(I.xbf.ptr, npad);                    // list kernel: 128-row boxes
+  const CUtensorMap mb256 = make_map(I.xbf.ptr, npad, FILTER_TN);      // filter: 256-row boxes
 
   // 1-2. thresholds and survivors
   DevBuf<float> tau((size_t)nq, s);
@@ -477,7 +480,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   int* ovf = cnt.ptr + nq;
   LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, (size_t)(nq + 1) * sizeof(int), s));
   DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
-  launch_filter_scan(ma, mb, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
+  launch_filter_scan(ma, mb256, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
 
   // 3. top-CT of the survivors
   DevBuf<uint64_t> best((size_t)nq * CT, s);
