@@ -333,6 +333,27 @@ def main():
         cpu_qps = sample / tcpu
         extras["cpu_baseline"] = {"value": cpu_qps, "unit": "queries/s", "cores": threads, "kind": "port",
                                   "sample": f"{sample} queries x {N_BASE} points (GoldStandard port)"}
+        # denominator of the headline ratio: the engine's own tuned FP32 SIMT exact scan
+        # (implementation 2) on the same GPU, same base, 1024 of the same queries
+        if args.path == "tc":
+            simt = L.Index(x, implementation=2, distanceFunc=1)
+            nsub = min(1024, N_QUERY)
+            qs_dev = qd[:nsub].contiguous()
+            outs = torch.empty((nsub, K, 2), dtype=torch.int32, device=dev)
+            for _ in range(2):
+                simt.query_device(qs_dev.data_ptr(), nsub, K, outs.data_ptr(), stream=sh)
+            torch.cuda.synchronize()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            simt.query_device(qs_dev.data_ptr(), nsub, K, outs.data_ptr(), stream=sh)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            simt_qps = nsub / (g0.elapsed_time(g1) / 1e3)
+            extras["denominators"] = {
+                "engine_simt_exact": {"value": simt_qps, "unit": "queries/s",
+                                      "sample": f"{nsub} queries x {N_BASE} points, FP32 SIMT exact scan"},
+                "ratio_value_over_simt": value / simt_qps}
+            del simt
         # serving: the same resident base behind the continuous-batching loop, mixed with
         # a 1024-bit SimHash index and a cross-polytope LSH index (L=32, K=2) of it
         if args.path == "tc":

@@ -80,6 +80,18 @@ struct FilterArgs {
   int* err;
 };
 
+// Move a row's staged survivors (score, id; stride BM in shared memory) to the query's
+// candidate array: one atomicAdd reserves the slots.
+__device__ __forceinline__ void flush_staged(int* cnt, uint64_t* dst, int cap, const float* ssc, const int* sid,
+                                          int& scnt) {
+  if (scnt > 0) {
+    const int base = atomicAdd(cnt, scnt);
+    for (int e = 0; e < scnt; ++e)
+      if (base + e < cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
+    scnt = 0;
+  }
+}
+
 template <int MODE, int GW>
 __global__ void __launch_bounds__(F_THREADS, 1)
     tc_filter_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
@@ -208,15 +220,6 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       const int qt = u % a.QT, c = u / a.QT;
       const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
       const int q = qt * BM + r;
-      auto flush = [&]() {
-        if (scnt > 0) {
-          const int base = atomicAdd(a.cnt + q, scnt);
-          uint64_t* dst = a.cand + (int64_t)q * a.cap;
-          for (int e = 0; e < scnt; ++e)
-            if (base + e < a.cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
-          scnt = 0;
-        }
-      };
       float tau = INFINITY;
       if (MODE == MODE_FILTER && q < a.nq) tau = a.tau ? a.tau[q] : -INFINITY;
       for (int p = p0; p < p1; ++p) {
@@ -269,7 +272,10 @@ __global__ void __launch_bounds__(F_THREADS, 1)
 #pragma unroll
             for (int gg = 0; gg < 8; ++gg) {
               if (!__any_sync(0xffffffffu, m[gg] >= tau)) continue;
-              if (m[gg] >= tau && scnt > F_SBUF - 8) flush();  // this group may add 8
+              int ng = 0;  // this lane's survivors in the group
+#pragma unroll
+              for (int jj = 0; jj < 8; ++jj) ng += __uint_as_float(v[8 * gg + jj]) >= tau ? 1 : 0;
+              if (scnt + ng > F_SBUF) flush_staged(a.cnt + q, a.cand + (int64_t)q * a.cap, a.cap, ssc, sid, scnt);
 #pragma unroll
               for (int jj = 0; jj < 8; ++jj) {
                 const float s = __uint_as_float(v[8 * gg + jj]);
@@ -283,7 +289,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           }
         }
       }
-      if (MODE == MODE_FILTER) flush();  // the next unit is another query tile
+      if (MODE == MODE_FILTER && scnt > 0)  // the next unit is another query tile
+        flush_staged(a.cnt + q, a.cand + (int64_t)q * a.cap, a.cap, ssc, sid, scnt);
     }
   }
 
