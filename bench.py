@@ -11,6 +11,18 @@ larger than the 129 MB L2, so no flush is needed between steps.
   --path exact    plain FP32 SIMT exact scan (the denominator of the speed-up)
   --path simhash  1024-bit SimHash + Hamming top-C + FP32 re-rank
 
+`--config` selects one of the measurement configurations instead of the headline (each
+prints its own line with its own metric; the headline is the default):
+
+  1       exact angular k-NN, N = 100k, d = 100, Q = 1000, k = 32 (--path exact or tc)
+  2       1024-bit SimHash, N = 1.2M, Q = 10k, C = 1024 candidates re-ranked (2-c128: C = 128)
+  3       tensor-core exact scan, N = 1M, d = 128 (100 + 28 zero dims), Q = 16,384
+  4a      cross-polytope LSH, L = 32 tables, K = 2 hashes a key, 3 rounds, N = 1M, d = 128
+          padded, Q = 10k, exact angular distance on candidates (4a-k1: K = 1)
+  4b      weighted MinHash, 256 byte samples, N = 500k, d = 100 sparse Gamma(2,1) values
+          (30% nonzero), Q = 10k, Jaccard sketch scan + generalized-Jaccard re-rank
+          (4b-1bit: 256 one-bit samples)
+
 `value` is whole-job queries/sec with queries and results resident in HBM; `e2e` is the
 same metric through the C ABI with host (pinned) buffers, copies inside the timed
 region.  `--impl reference` times the reference's CPU brute force (a port of
@@ -36,6 +48,22 @@ sys.path.insert(0, ROOT)
 
 METRIC = "queries/sec at recall@32>=0.99 on 1.2Mx100 (TC+serving vs plain scan)"
 N_BASE, DIM, N_QUERY, K = 1_200_000, 100, 10_000, 32
+PAD_DIM = 0        # zero dimensions appended to every vector
+DATA = "clustered"  # or "sparse" (weighted MinHash configuration)
+CAND = 1024         # SimHash candidates re-ranked
+CP_HASHES = 2       # cross-polytope hashes a key
+
+# measurement configurations: path and shape overrides
+CONFIGS = {
+    "1": dict(path="exact", N_BASE=100_000, N_QUERY=1000),
+    "2": dict(path="simhash", CAND=1024),
+    "2-c128": dict(path="simhash", CAND=128),
+    "3": dict(path="tc", N_BASE=1_000_000, N_QUERY=16_384, PAD_DIM=28),
+    "4a": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=2),
+    "4a-k1": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=1),
+    "4b": dict(path="wmh", N_BASE=500_000, DATA="sparse"),
+    "4b-1bit": dict(path="wmh1", N_BASE=500_000, DATA="sparse"),
+}
 
 
 def peaks():
@@ -97,8 +125,15 @@ class ClockSampler:
 def make_data(seed_offset: int):
     from lshongpu_gb300 import datasets
 
-    x = datasets.clustered(N_BASE, DIM, seed=100 + seed_offset)
-    q = datasets.clustered(N_QUERY, DIM, seed=101 + seed_offset)
+    if DATA == "sparse":
+        x = datasets.sparse_gamma(N_BASE, DIM, seed=100 + seed_offset)
+        q = datasets.sparse_gamma(N_QUERY, DIM, seed=101 + seed_offset)
+    else:
+        x = datasets.clustered(N_BASE, DIM, seed=100 + seed_offset)
+        q = datasets.clustered(N_QUERY, DIM, seed=101 + seed_offset)
+    if PAD_DIM:
+        x = np.ascontiguousarray(np.pad(x, ((0, 0), (0, PAD_DIM))))
+        q = np.ascontiguousarray(np.pad(q, ((0, 0), (0, PAD_DIM))))
     return x, q
 
 
@@ -108,17 +143,38 @@ def build_index(L, x, path: str):
     if path == "exact":
         return L.Index(x, implementation=2, distanceFunc=1)
     if path == "simhash":
-        return L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=1024))
+        return L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=CAND))
+    if path == "cplsh":
+        return L.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7,
+                       bucketKeyBits=8 * CP_HASHES, tables=32, options=L.make_options(cp_hashes=CP_HASHES))
+    if path == "wmh":
+        return L.Index(x, implementation=4, distanceFunc=2, sketchDim=256)
+    if path == "wmh1":
+        return L.Index(x, implementation=5, distanceFunc=2, sketchDim=8)
     raise SystemExit(f"unknown path {path}")
 
 
+# FP32 SIMT peak (no measured figure exists for it): 152 SMs x 128 FMA/clk x 2 x 2.07 GHz
+FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
 def algorithmic(path: str, prof: dict, nq: int):
-    """(kernel, bound, work per launch, unit) for the dominant kernel of the path."""
+    """(kernel, bound, work per launch, unit) for the dominant kernel of the path.  FLOPs
+    count the index dimension (100 at the headline: the kernel's own padding to 112/128 is
+    not counted; 128 at configuration 3, whose vectors carry 28 zero dimensions); sketch
+    scans count the sketch bytes streamed once per batch."""
+    d = DIM
     if path == "tc":
-        return "tc_filter", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
+        return "tc_filter", "tensor", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
     if path == "exact":
-        return "scan_float", "tensor", 2.0 * nq * N_BASE * DIM / 1e12, "TFLOP/s"
-    return "scan_bits", "hbm", N_BASE * 128 / 1e9, "GB/s"
+        return "scan_float", "fp32", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
+    if path == "simhash":
+        return "scan_bits", "hbm", N_BASE * 128 / 1e9, "GB/s"
+    if path == "wmh":
+        return "scan_bits", "hbm", N_BASE * 256 / 1e9, "GB/s"
+    if path == "wmh1":
+        return "scan_bits", "hbm", N_BASE * 32 / 1e9, "GB/s"
+    return "lsh_query", "gather", None, None
 
 
 def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7) -> dict:
@@ -135,6 +191,14 @@ def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7
     for i, ix in indexes.items():
         srv.add_index(i, ix)
     ids = list(indexes)
+    # untimed warm-up: record every (index, k, power-of-two batch class) graph once
+    for which in ids:
+        for k in (10, 32, 100):
+            size = 1
+            while size <= 4096:
+                srv.wait(srv.submit(which, pool[:size], k))
+                size *= 2
+    st0 = srv.stats()
     mean_size = (4096 - 1) / np.log(4096.0)
     req_rate = rate_qps / mean_size
     tickets, lat, sizes = [], [], []
@@ -177,8 +241,21 @@ def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7
     lat_a = np.array(lat)
     return {"offered_qps": rate_qps, "achieved_qps": sum(sizes) / wall, "requests": len(tickets),
             "p50_ms": float(np.percentile(lat_a, 50)), "p99_ms": float(np.percentile(lat_a, 99)),
-            "p999_ms": float(np.percentile(lat_a, 99.9)), "launches": st["launches"],
-            "graph_replays": st["graph_replays"], "rejected": st["rejected"]}
+            "p999_ms": float(np.percentile(lat_a, 99.9)), "launches": st["launches"] - st0["launches"],
+            "graph_replays": st["graph_replays"] - st0["graph_replays"], "rejected": st["rejected"] - st0["rejected"]}
+
+
+def workload_text(args) -> str:
+    d = f"{DIM}" if not PAD_DIM else f"{DIM + PAD_DIM} ({DIM} + {PAD_DIM} zero dims)"
+    data = ("sparse Gamma(2,1) values, 30% nonzero" if DATA == "sparse"
+            else "clustered unit vectors (1000 clusters, sigma 0.05)")
+    what = {"tc": "tensor-core exact scan", "exact": "FP32 SIMT exact scan",
+            "simhash": f"1024-bit SimHash, {CAND} candidates re-ranked",
+            "cplsh": f"cross-polytope LSH, L=32, K={CP_HASHES}, 3 rounds, exact angular on candidates",
+            "wmh": "weighted MinHash, 256 byte samples, Jaccard scan + generalized-Jaccard re-rank",
+            "wmh1": "weighted MinHash, 256 one-bit samples, Jaccard scan + generalized-Jaccard re-rank"}[args.path]
+    cfg = f"configuration {args.config}: " if args.config else ""
+    return f"{cfg}{what}: N={N_BASE}, d={d}, Q={N_QUERY}, k={K}, {data}"
 
 
 def run_reference_arm(args, world, rank):
@@ -217,13 +294,21 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--path", default="tc", choices=["tc", "exact", "simhash"])
+    ap.add_argument("--path", default=None, choices=["tc", "exact", "simhash", "cplsh", "wmh", "wmh1"])
+    ap.add_argument("--config", default=None, choices=sorted(CONFIGS), help="measurement configuration")
     ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
     ap.add_argument("--n", type=int, default=N_BASE, help="base size (profiling cases only)")
     ap.add_argument("--nq", type=int, default=N_QUERY, help="queries per step (profiling cases only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     globals().update(N_BASE=args.n, N_QUERY=args.nq)
+    if args.config:
+        over = dict(CONFIGS[args.config])
+        path = over.pop("path")
+        args.path = args.path or path
+        globals().update(over)
+        globals()["METRIC"] = f"queries/sec, configuration {args.config}"
+    args.path = args.path or "tc"
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -306,14 +391,22 @@ def main():
     hbm, bf16, bf16s, peak_kind = peaks()
     kname, bound, work, unit = algorithmic(args.path, prof, N_QUERY)
     cnt, kms = prof.get(kname, (0, 0.0))
-    achieved = (work / (kms / cnt / 1e3)) if cnt else None
-    if unit == "GB/s":
-        work_unit, peak = work, hbm
+    achieved = (work / (kms / cnt / 1e3)) if (cnt and work) else None
+    if bound == "hbm":
+        peak = hbm
+    elif bound == "fp32":
+        peak, peak_kind = FP32_SIMT_NOMINAL_TFLOPS, "nominal (152 SMs x 128 FMA/clk x 2 x 2.07 GHz)"
+    elif bound == "tensor":
+        peak = bf16
     else:
-        work_unit, peak = work, bf16
+        peak = None
+    # DRAM bytes of one tc_filter launch at the headline shape, from the committed ncu
+    # capture (profiles/tc_filter_1.2Mx100_q10k_dram.md): the base once + survivors
+    traffic = 310.21e6 + 36.82e6 if (args.config is None and args.path == "tc" and N_BASE == 1_200_000
+                                     and N_QUERY == 10_000) else None
     roofline = {"bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": unit,
-                "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-                "traffic": None, "kernel_ms_per_launch": (kms / cnt) if cnt else None,
+                "frac": (achieved / peak) if (achieved and peak) else None, "peak_source": peak_kind,
+                "traffic": traffic, "traffic_unit": "bytes per launch" if traffic else None, "kernel_ms_per_launch": (kms / cnt) if cnt else None,
                 "kernel_share": (kms / sum(v[1] for v in prof.values())) if prof else None}
 
     extras = {}
@@ -322,17 +415,23 @@ def main():
 
         threads = os.cpu_count() or 1
         res = out.cpu().numpy().view(np.int32)[:, :, 0]
-        nchk = 200
-        tids, _ = oracle.fp64_topk(x, q[:nchk], K, threads=threads)
+        headline = args.config is None and args.path == "tc"
+        if DATA == "sparse":  # generalized-Jaccard truth (single-threaded oracle: small sample)
+            nchk = 50
+            tids, _ = oracle.exact_topk(x, q[:nchk], K, dist=2)
+        else:
+            nchk = 200
+            tids, _ = oracle.fp64_topk(x, q[:nchk], K, threads=threads)
         rec = np.mean([len(set(res[i].tolist()) & set(tids[i].tolist())) / K for i in range(nchk)])
         extras["recall_at_32"] = float(rec)
         extras["recall_queries"] = nchk
         # CPU baseline: GoldStandard port, bounded sample, all host threads
-        sample = 2 * threads
-        _, _, tcpu = oracle.goldstandard(x, q[:sample], K, threads)
-        cpu_qps = sample / tcpu
-        extras["cpu_baseline"] = {"value": cpu_qps, "unit": "queries/s", "cores": threads, "kind": "port",
-                                  "sample": f"{sample} queries x {N_BASE} points (GoldStandard port)"}
+        if DATA != "sparse":
+            sample = 2 * threads
+            _, _, tcpu = oracle.goldstandard(x, q[:sample], K, threads)
+            cpu_qps = sample / tcpu
+            extras["cpu_baseline"] = {"value": cpu_qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                                      "sample": f"{sample} queries x {N_BASE} points (GoldStandard port)"}
         # denominator of the headline ratio: the engine's own tuned FP32 SIMT exact scan
         # (implementation 2) on the same GPU, same base, 1024 of the same queries
         if args.path == "tc":
@@ -356,7 +455,7 @@ def main():
             del simt
         # serving: the same resident base behind the continuous-batching loop, mixed with
         # a 1024-bit SimHash index and a cross-polytope LSH index (L=32, K=2) of it
-        if args.path == "tc":
+        if headline:
             serve_ix = {0: idx,
                         1: L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=1024)),
                         2: L.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7,
@@ -368,13 +467,13 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16" if args.path == "tc" else ("u32" if args.path == "simhash" else "f32"),
+        "vs_baseline": None,
+        "dtype": {"tc": "bf16", "simhash": "u32", "wmh": "u8", "wmh1": "u32"}.get(args.path, "f32"),
         "data": "synthetic",
-        "config": {"workload": f"k-NN path={args.path}: N={N_BASE}, d={DIM}, Q={N_QUERY}, k={K}, clustered unit "
-                               f"vectors (1000 clusters, sigma 0.05)", "global_batch": N_QUERY * world,
+        "config": {"workload": workload_text(args), "global_batch": N_QUERY * world,
                    "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
         "roofline": roofline,
-        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERY * DIM * 4,
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERY * (DIM + PAD_DIM) * 4,
                 "d2h_bytes_per_step": N_QUERY * K * 8},
         "gpu_launches": launches,
         "clocks": clk.summary(),
