@@ -21,7 +21,6 @@ namespace lshg {
 namespace {
 
 constexpr int kTile = 128;      // points per tile (one per thread of each half)
-constexpr int kBuf = 256;
 constexpr int kMaxChunks = 16;  // up to 64 words (2048 bits) per sketch
 
 struct BitsSmem {
@@ -35,7 +34,7 @@ __host__ __device__ inline size_t smem_take(size_t& off, size_t bytes) {
   return at;
 }
 
-__host__ __device__ inline BitsSmem bits_layout(int wp, int QB, int C) {
+__host__ __device__ inline BitsSmem bits_layout(int wp, int QB, int C, int kBuf) {
   BitsSmem L;
   size_t off = 0;
   L.qs = smem_take(off, (size_t)QB * wp * 4);
@@ -59,15 +58,22 @@ __device__ __forceinline__ int word_score(uint32_t a, uint32_t b) {
   return __popc(a ^ b);
 }
 
-template <int OP, int QB>
-__global__ void __launch_bounds__(256) scan_bits_kernel(const uint32_t* __restrict__ xs, int64_t n, int wp, int words,
+// QB queries a CTA; each query's append buffer holds KBUF keys and the CTA checks the
+// buffers every T tiles: a tile adds at most kTile keys to a query's buffer, so folding
+// every buffer above KBUF - T * kTile at each check means no buffer can overflow between
+// checks.  The check is one __syncthreads_or on "one of my appends landed above the
+// limit" -- no block barrier in between.
+template <int OP, int QB, int KBUF, int T>
+__global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __restrict__ xs, int64_t n, int wp, int words,
                                                         int sbytes, const uint32_t* __restrict__ qs, int nq, int C,
                                                         int tiles_per_split, int splits, uint64_t* __restrict__ out) {
+  static_assert(KBUF >= T * kTile, "append buffer must absorb T tiles");
+  constexpr int kLimit = KBUF - T * kTile;
   extern __shared__ __align__(16) unsigned char smem[];
-  const BitsSmem L = bits_layout(wp, QB, C);
+  const BitsSmem L = bits_layout(wp, QB, C, KBUF);
   uint32_t* qsm = reinterpret_cast<uint32_t*>(smem + L.qs);
   TopCShared S{reinterpret_cast<uint64_t*>(smem + L.kept), reinterpret_cast<uint64_t*>(smem + L.buf),
-               reinterpret_cast<int*>(smem + L.cnt), reinterpret_cast<uint64_t*>(smem + L.thr), C, kBuf};
+               reinterpret_cast<int*>(smem + L.cnt), reinterpret_cast<uint64_t*>(smem + L.thr), C, KBUF};
 
   const int q0 = blockIdx.x * QB;
   const int split = blockIdx.y;
@@ -91,6 +97,7 @@ __global__ void __launch_bounds__(256) scan_bits_kernel(const uint32_t* __restri
   for (int a = 0; a < QPT; ++a) thr[a] = kEmptyKey;
 
   const float inv_div_f = (OP == OP_ONEBIT_JACCARD) ? (float)(32 * words) : (float)sbytes;
+  bool over = false;  // one of this thread's appends since the last check landed above kLimit
 
   for (int tile = t_begin; tile < t_end; ++tile) {
     const int64_t p = (int64_t)tile * kTile + pl;
@@ -123,14 +130,24 @@ __global__ void __launch_bounds__(256) scan_bits_kernel(const uint32_t* __restri
         } else {
           dist = __fsub_rn(1.0f, __fdiv_rn((float)acc, inv_div_f));
         }
-        topc_push(S, qi, make_key(dist, (int)p), thr[a]);
+        const uint64_t key = make_key(dist, (int)p);
+        if (key < thr[a]) {
+          const int pos = atomicAdd(&S.cnt[qi], 1);
+          S.buf[(size_t)qi * KBUF + pos] = key;
+          over |= pos >= kLimit;
+        }
       }
     }
-    topc_flush(S, QB, kBuf - kTile);
+    if ((tile - t_begin) % T == T - 1 && tile + 1 < t_end) {  // uniform: same tile loop in every thread
+      if (__syncthreads_or(over)) {
+        topc_flush(S, QB, kLimit);
 #pragma unroll
-    for (int a = 0; a < QPT; ++a) {
-      const int qi = half + 2 * a;
-      if (qi < QB) thr[a] = S.thr[qi];
+        for (int a = 0; a < QPT; ++a) {
+          const int qi = half + 2 * a;
+          if (qi < QB) thr[a] = S.thr[qi];
+        }
+      }
+      over = false;
     }
   }
   topc_flush(S, QB, 0);
@@ -141,12 +158,12 @@ __global__ void __launch_bounds__(256) scan_bits_kernel(const uint32_t* __restri
   }
 }
 
-template <int OP, int QB>
+template <int OP, int QB, int KBUF, int T>
 void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                 int splits, uint64_t* out, cudaStream_t s) {
   ProfScope _ps("scan_bits", s);
-  size_t smem = bits_layout(wp, QB, C).total;
-  auto kern = scan_bits_kernel<OP, QB>;
+  size_t smem = bits_layout(wp, QB, C, KBUF).total;
+  auto kern = scan_bits_kernel<OP, QB, KBUF, T>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int ntiles = ceil_div(n, kTile);
   int tps = ceil_div(ntiles, splits);
@@ -159,9 +176,9 @@ void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, co
 template <int OP>
 void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                int splits, uint64_t* out, cudaStream_t s) {
-  if (C <= 128) launch_cfg<OP, 32>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else if (C <= 1024) launch_cfg<OP, 8>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else launch_cfg<OP, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  if (C <= 128) launch_cfg<OP, 32, 256, 1>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else if (C <= 1024) launch_cfg<OP, 8, 512, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else launch_cfg<OP, 2, 1024, 4>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
 }
 
 }  // namespace

@@ -110,9 +110,11 @@ def test_simhash_sketch_bits(engine, orc, words):
     assert np.array_equal(qs, orc.simhash(q, planes, words, 32))
 
 
-@pytest.mark.parametrize("C", [128, 4096])
-def test_simhash_scan_rerank(engine, orc, C):
-    n, nq, words = 6000, 21, 8
+# C picks the scan's layout: 32, 8 or 2 queries a CTA with append buffers checked every
+# 1, 2 or 4 tiles
+@pytest.mark.parametrize("C,n", [(128, 6000), (256, 6000), (1024, 6000), (1024, 40000), (4096, 6000)])
+def test_simhash_scan_rerank(engine, orc, C, n):
+    nq, words = 21, 8
     x, q = data(n, nq)
     opt = engine.make_options(candidates=C)
     r = engine.linear_scans(3, 32, D, nq, n, x, q, words, 1, options=opt)
