@@ -46,13 +46,24 @@ __device__ __forceinline__ uint64_t global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
+// try_wait that may suspend the thread until the phase completes or `hint_ns` passes, so
+// waiting warps do not take issue slots from the working ones.
+__device__ __forceinline__ bool mbar_try_sleep(uint32_t bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
 // Bounded wait: gives up when another role aborted (unless `ignore_abort`) or after
 // kWaitNs, raising the CTA's abort flag.
 static __device__ __noinline__ bool mbar_wait_slow(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                             bool ignore_abort) {
   const uint64_t t0 = global_ns();
   while (true) {
-    if (mbar_try(bar, parity)) return true;
+    if (mbar_try_sleep(bar, parity, 20000u)) return true;
     if (!ignore_abort && *abort_flag) return false;
     if (global_ns() - t0 > kWaitNs) {
       *abort_flag = 1;

@@ -458,7 +458,9 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   using namespace tc;
   if (nq <= 0) return;
   LSHG_REQUIRE(k <= 128, "tensor-core scan: k must be <= 128");
-  const int CT = k <= 64 ? 64 : 128;
+  // candidates re-ranked a query: at least twice k up to k = 64 (BF16 scores can swap
+  // near-equal neighbours at the boundary); 128 (the list kernel's maximum) beyond
+  const int CT = k <= 32 ? 64 : 128;
   const int64_t qpad = (int64_t)ceil_div(nq, BM) * BM;
   const int QT = (int)(qpad / BM);
   FilterPlan plan = plan_filter(I.n, CT);

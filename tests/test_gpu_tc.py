@@ -112,3 +112,23 @@ def test_tc_overflow_duplicates(engine, orc):
     assert recall(res["ID"], ids) >= 0.99
     a, b = _query_both_paths(idx, q, 32)
     assert np.array_equal(a["ID"], b["ID"]) and np.array_equal(a["distance"], b["distance"])
+
+
+@pytest.mark.parametrize("n,nq,k,d", [(3000, 1, 1, 100), (3000, 5, 64, 37), (9000, 130, 65, 128), (20, 9, 32, 100),
+                                      (70000, 200, 10, 64)])
+def test_tc_edge_shapes(engine, orc, n, nq, k, d):
+    """Odd and full-width dimensions (7 or 8 MMA K steps, or 3 for d = 37), a single
+    query, k at the 64 / 128 candidate switch, a base smaller than k (missing results are
+    (-1, 2^31) as in the reference) and a batch that is not a multiple of 128 rows."""
+    x = datasets.clustered(n, d, 131, count=20)
+    q = datasets.clustered(nq, d, 132, count=20)
+    idx = engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=1)
+    res = idx.query(q, k)
+    kk = min(k, n)
+    ids, ds = orc.exact_topk(x, q, kk, dist=1)
+    assert recall(res["ID"][:, :kk], ids) >= 0.99
+    if n < k:
+        assert np.all(res["ID"][:, n:] == -1)
+        assert np.all(res["distance"][:, n:] == np.float32(2.0 ** 31))
+    a, b = _query_both_paths(idx, q, k)
+    assert np.array_equal(a["ID"], b["ID"]) and np.array_equal(a["distance"], b["distance"])
