@@ -63,7 +63,9 @@ __device__ __forceinline__ int word_score(uint32_t a, uint32_t b) {
 // every buffer above KBUF - T * kTile at each check means no buffer can overflow between
 // checks.  The check is one __syncthreads_or on "one of my appends landed above the
 // limit" -- no block barrier in between.
-template <int OP, int QB, int KBUF, int T>
+// NC > 0: rows of exactly NC 128-bit chunks, loops fully unrolled without bounds tests;
+// NC = 0: any row width up to kMaxChunks chunks (runtime bound).
+template <int OP, int QB, int KBUF, int T, int NC>
 __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __restrict__ xs, int64_t n, int wp, int words,
                                                         int sbytes, const uint32_t* __restrict__ qs, int nq, int C,
                                                         int tiles_per_split, int splits, uint64_t* __restrict__ out) {
@@ -80,7 +82,8 @@ __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __res
   const int ntiles = (int)((n + kTile - 1) / kTile);
   const int t_begin = split * tiles_per_split;
   const int t_end = min(ntiles, t_begin + tiles_per_split);
-  const int nc = wp >> 2;
+  constexpr int NCH = NC > 0 ? NC : kMaxChunks;
+  const int nc = NC > 0 ? NC : (wp >> 2);
 
   for (int i = threadIdx.x; i < QB * wp; i += blockDim.x) {
     int qi = i / wp;
@@ -102,10 +105,10 @@ __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __res
   for (int tile = t_begin; tile < t_end; ++tile) {
     const int64_t p = (int64_t)tile * kTile + pl;
     const bool valid = p < n;
-    uint4 xr[kMaxChunks];
+    uint4 xr[NCH];
     const uint4* row = reinterpret_cast<const uint4*>(xs + (valid ? p : 0) * wp);
 #pragma unroll
-    for (int c = 0; c < kMaxChunks; ++c) xr[c] = (c < nc && valid) ? __ldg(&row[c]) : make_uint4(0, 0, 0, 0);
+    for (int c = 0; c < NCH; ++c) xr[c] = ((NC > 0 || c < nc) && valid) ? __ldg(&row[c]) : make_uint4(0, 0, 0, 0);
 
     if (valid) {
 #pragma unroll
@@ -115,8 +118,8 @@ __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __res
         const uint4* qv = reinterpret_cast<const uint4*>(qsm + qi * wp);
         int acc = 0;
 #pragma unroll
-        for (int c = 0; c < kMaxChunks; ++c) {
-          if (c < nc) {
+        for (int c = 0; c < NCH; ++c) {
+          if (NC > 0 || c < nc) {
             uint4 b = qv[c];
             acc += word_score<OP>(xr[c].x, b.x) + word_score<OP>(xr[c].y, b.y) + word_score<OP>(xr[c].z, b.z) +
                    word_score<OP>(xr[c].w, b.w);
@@ -158,12 +161,12 @@ __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __res
   }
 }
 
-template <int OP, int QB, int KBUF, int T>
+template <int OP, int QB, int KBUF, int T, int NC>
 void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                 int splits, uint64_t* out, cudaStream_t s) {
   ProfScope _ps("scan_bits", s);
   size_t smem = bits_layout(wp, QB, C, KBUF).total;
-  auto kern = scan_bits_kernel<OP, QB, KBUF, T>;
+  auto kern = scan_bits_kernel<OP, QB, KBUF, T, NC>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int ntiles = ceil_div(n, kTile);
   int tps = ceil_div(ntiles, splits);
@@ -173,12 +176,22 @@ void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, co
   LSHG_CHECK_LAUNCH();
 }
 
-template <int OP>
+template <int OP, int NC>
 void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                int splits, uint64_t* out, cudaStream_t s) {
-  if (C <= 128) launch_cfg<OP, 32, 256, 1>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else if (C <= 1024) launch_cfg<OP, 8, 512, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else launch_cfg<OP, 2, 1024, 4>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  if (C <= 128) launch_cfg<OP, 32, 256, 1, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else if (C <= 1024) launch_cfg<OP, 8, 512, 2, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else launch_cfg<OP, 2, 1024, 4, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+}
+
+// Row width specialised for each sketch type's usual size (1024-bit SimHash = 8 chunks,
+// 256 byte samples = 16 chunks, 256 one-bit samples = 2 chunks); other widths use the
+// generic kernel.
+template <int OP, int NC_FAST>
+void launch_width(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
+                  int splits, uint64_t* out, cudaStream_t s) {
+  if (wp / 4 == NC_FAST) launch_op<OP, NC_FAST>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else launch_op<OP, 0>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
 }
 
 }  // namespace
@@ -199,9 +212,11 @@ int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbyte
   LSHG_REQUIRE(wp % 4 == 0 && wp / 4 <= kMaxChunks, "sketch scan: rows must be 4..64 words, multiple of 4");
   LSHG_REQUIRE(C >= 32 && C <= 4096 && (C & (C - 1)) == 0, "sketch scan: C must be a power of two in [32, 4096]");
   switch (op) {
-    case OP_HAMMING: launch_op<OP_HAMMING>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
-    case OP_BYTE_JACCARD: launch_op<OP_BYTE_JACCARD>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
-    case OP_ONEBIT_JACCARD: launch_op<OP_ONEBIT_JACCARD>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    case OP_HAMMING: launch_width<OP_HAMMING, 8>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    case OP_BYTE_JACCARD: launch_width<OP_BYTE_JACCARD, 16>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    case OP_ONEBIT_JACCARD:
+      launch_width<OP_ONEBIT_JACCARD, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+      break;
     default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "sketch scan: invalid sketch type");
   }
   return splits;

@@ -111,10 +111,11 @@ def test_simhash_sketch_bits(engine, orc, words):
 
 
 # C picks the scan's layout: 32, 8 or 2 queries a CTA with append buffers checked every
-# 1, 2 or 4 tiles
-@pytest.mark.parametrize("C,n", [(128, 6000), (256, 6000), (1024, 6000), (1024, 40000), (4096, 6000)])
-def test_simhash_scan_rerank(engine, orc, C, n):
-    nq, words = 21, 8
+# 1, 2 or 4 tiles; 32 words (1024 bits) runs the width-specialised kernel, 8 the generic one
+@pytest.mark.parametrize("C,n,words", [(128, 6000, 8), (256, 6000, 8), (1024, 6000, 8), (1024, 40000, 8),
+                                       (4096, 6000, 8), (128, 6000, 32), (1024, 20000, 32), (4096, 6000, 32)])
+def test_simhash_scan_rerank(engine, orc, C, n, words):
+    nq = 21
     x, q = data(n, nq)
     opt = engine.make_options(candidates=C)
     r = engine.linear_scans(3, 32, D, nq, n, x, q, words, 1, options=opt)
@@ -157,8 +158,9 @@ def wmh_oracle(orc, x, q, H, uniforms, onebit, words=0):
     return xs, qs, skx, skq
 
 
-def test_wmh_byte_sketch_and_scan(engine, orc, uniforms):
-    n, nq, S = 2000, 9, 64
+@pytest.mark.parametrize("S", [64, 256])  # 256 samples: the width-specialised scan
+def test_wmh_byte_sketch_and_scan(engine, orc, uniforms, S):
+    n, nq = 2000, 9
     x = datasets.sparse_gamma(n, D, 7)
     q = datasets.sparse_gamma(nq, D, 8)
     xs, qs, skx, skq = wmh_oracle(orc, x, q, S, uniforms, 0)
@@ -172,8 +174,9 @@ def test_wmh_byte_sketch_and_scan(engine, orc, uniforms):
     assert np.array_equal(r.distances, ds)
 
 
-def test_wmh_onebit_sketch_and_scan(engine, orc, uniforms):
-    n, nq, W = 2000, 9, 4
+@pytest.mark.parametrize("W", [4, 8])  # 8 words: the width-specialised scan
+def test_wmh_onebit_sketch_and_scan(engine, orc, uniforms, W):
+    n, nq = 2000, 9
     x = datasets.sparse_gamma(n, D, 9)
     q = datasets.sparse_gamma(nq, D, 10)
     xs, qs, skx, skq = wmh_oracle(orc, x, q, W * 32, uniforms, 1, W)
