@@ -37,10 +37,10 @@ __host__ __device__ inline size_t smem_take(size_t& off, size_t bytes) {
   return at;
 }
 
-__host__ __device__ inline FloatScanSmem float_scan_layout(int d, int QB, int C) {
+__host__ __device__ inline FloatScanSmem float_scan_layout(int d, int QB, int C, int nbuf) {
   FloatScanSmem L;
   size_t off = 0;
-  L.xs = smem_take(off, (size_t)kTile * d * 4);
+  L.xs = smem_take(off, (size_t)nbuf * kTile * d * 4);  // point tile, double-buffered when it fits
   L.qs = smem_take(off, (size_t)QB * d * 4);
   L.qn = smem_take(off, (size_t)QB * 4);
   L.kept = smem_take(off, (size_t)QB * C * 8);
@@ -59,12 +59,22 @@ __device__ __forceinline__ float finish_distance(float a, float b, float qn, flo
   return a;  // DIST_SQEUCLID
 }
 
+// 16-byte asynchronous global -> shared copy (L2 only) and its group fences.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 template <int DIST, int QB, int MQ>
 __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
     const float* __restrict__ xt, int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
-    int nq, const float* __restrict__ qnorm, int C, int tiles_per_split, int splits, uint64_t* __restrict__ out) {
+    int nq, const float* __restrict__ qnorm, int C, int tiles_per_split, int splits, int nbuf,
+    uint64_t* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const FloatScanSmem L = float_scan_layout(d, QB, C);
+  const FloatScanSmem L = float_scan_layout(d, QB, C, nbuf);
   float* xs = reinterpret_cast<float*>(smem + L.xs);
   float* qs = reinterpret_cast<float*>(smem + L.qs);
   float* qn = reinterpret_cast<float*>(smem + L.qn);
@@ -92,11 +102,27 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
 #pragma unroll
   for (int a = 0; a < MQ; ++a) thr[a] = kEmptyKey;
 
-  for (int tile = t_begin; tile < t_end; ++tile) {
+  // with two buffers the copy of tile t+1 runs while tile t is scored; with one (large d)
+  // each tile is copied, then scored
+  const int tile_f4 = kTile * d / 4;
+  auto slot = [&](int tile) { return nbuf == 2 ? (tile & 1) : 0; };
+  auto issue_tile = [&](int tile) {
     const float4* src = reinterpret_cast<const float4*>(xt + (int64_t)tile * kTile * d);
-    float4* dst = reinterpret_cast<float4*>(xs);
-    for (int i = threadIdx.x; i < kTile * d / 4; i += blockDim.x) dst[i] = src[i];
+    float4* dst = reinterpret_cast<float4*>(xs) + (size_t)slot(tile) * tile_f4;
+    for (int i = threadIdx.x; i < tile_f4; i += blockDim.x) cp_async16(dst + i, src + i);
+    cp_async_commit();
+  };
+  if (t_begin < t_end) issue_tile(t_begin);
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    if (nbuf == 2 && tile + 1 < t_end) {
+      issue_tile(tile + 1);  // its buffer was last read by tile - 1, finished at the previous flush
+      cp_async_wait<1>();
+    } else {
+      if (nbuf == 1 && tile > t_begin) issue_tile(tile);  // the previous flush ended every read
+      cp_async_wait<0>();
+    }
     __syncthreads();
+    const float* xcur = xs + (size_t)slot(tile) * kTile * d;
 
     float acc[MQ][4];
     float acc2[MQ][4];
@@ -106,7 +132,7 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
       for (int b = 0; b < 4; ++b) { acc[a][b] = 0.0f; acc2[a][b] = 0.0f; }
 
     for (int j = 0; j < d; ++j) {
-      float4 xv = *reinterpret_cast<const float4*>(&xs[j * kTile + 4 * tp]);
+      float4 xv = *reinterpret_cast<const float4*>(&xcur[j * kTile + 4 * tp]);
       float xb[4] = {xv.x, xv.y, xv.z, xv.w};
       float qa[MQ];
       if (MQ == 4) {
@@ -160,28 +186,30 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
 }
 
 struct FloatCfg {
-  int QB, MQ;
+  int QB, MQ, nbuf;
 };
 
 FloatCfg pick_float_cfg(int d, int C) {
   const size_t cap = 220 * 1024;
-  if (C <= 128 && float_scan_layout(d, 32, C).total <= cap) return {32, 4};
-  if (C <= 1024 && float_scan_layout(d, 8, C).total <= cap) return {8, 1};
-  if (float_scan_layout(d, 2, C).total <= cap) return {2, 1};
+  for (int nbuf = 2; nbuf >= 1; --nbuf) {
+    if (C <= 128 && float_scan_layout(d, 32, C, nbuf).total <= cap) return {32, 4, nbuf};
+    if (C <= 1024 && float_scan_layout(d, 8, C, nbuf).total <= cap) return {8, 1, nbuf};
+    if (float_scan_layout(d, 2, C, nbuf).total <= cap) return {2, 1, nbuf};
+  }
   throw Error(LSHG_ERR_UNSUPPORTED, "float scan: dimension / candidate count too large for shared memory");
 }
 
 template <int DIST, int QB, int MQ>
 void launch_cfg(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq, const float* qnorm,
-                int C, int splits, uint64_t* out, cudaStream_t s) {
+                int C, int splits, int nbuf, uint64_t* out, cudaStream_t s) {
   ProfScope _ps("scan_float", s);
-  size_t smem = float_scan_layout(d, QB, C).total;
+  size_t smem = float_scan_layout(d, QB, C, nbuf).total;
   auto kern = scan_float_kernel<DIST, QB, MQ>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int ntiles = ceil_div(n, kTile);
   int tps = ceil_div(ntiles, splits);
   dim3 grid(ceil_div(nq, QB), splits);
-  kern<<<grid, (QB / MQ) * 32, smem, s>>>(xt, n, d, xnorm, q, nq, qnorm, C, tps, splits, out);
+  kern<<<grid, (QB / MQ) * 32, smem, s>>>(xt, n, d, xnorm, q, nq, qnorm, C, tps, splits, nbuf, out);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
@@ -190,9 +218,9 @@ template <int DIST>
 void launch_dist(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq, const float* qnorm,
                  int C, int splits, uint64_t* out, cudaStream_t s) {
   FloatCfg c = pick_float_cfg(d, C);
-  if (c.QB == 32) launch_cfg<DIST, 32, 4>(xt, n, d, xnorm, q, nq, qnorm, C, splits, out, s);
-  else if (c.QB == 8) launch_cfg<DIST, 8, 1>(xt, n, d, xnorm, q, nq, qnorm, C, splits, out, s);
-  else launch_cfg<DIST, 2, 1>(xt, n, d, xnorm, q, nq, qnorm, C, splits, out, s);
+  if (c.QB == 32) launch_cfg<DIST, 32, 4>(xt, n, d, xnorm, q, nq, qnorm, C, splits, c.nbuf, out, s);
+  else if (c.QB == 8) launch_cfg<DIST, 8, 1>(xt, n, d, xnorm, q, nq, qnorm, C, splits, c.nbuf, out, s);
+  else launch_cfg<DIST, 2, 1>(xt, n, d, xnorm, q, nq, qnorm, C, splits, c.nbuf, out, s);
 }
 
 }  // namespace

@@ -50,6 +50,18 @@ def test_exact_angular_bit_exact(engine, orc, n, nq, k):
     assert np.array_equal(r.distances, ds)
 
 
+@pytest.mark.parametrize("d,n", [(300, 3000), (64, 20000)])
+def test_exact_angular_dims(engine, orc, d, n):
+    """d = 300 does not fit two point tiles in shared memory and runs the single-buffered
+    scan; d = 64 with 157 tiles exercises the double-buffered pipeline over many tiles."""
+    nq = 40
+    x, q = data(n, nq, seed=17, d=d)
+    r = engine.linear_scans(2, 32, d, nq, n, x, q, 0, 1)
+    ids, ds = orc.exact_topk(x, q, 32, dist=1)
+    assert np.array_equal(r.ids, ids)
+    assert np.array_equal(r.distances, ds)
+
+
 def test_exact_ties_lower_index_and_short_base(engine, orc):
     x, q = data(40, 5)
     x = np.concatenate([x, x[:10]])  # exact duplicates: equal distances, lower id first
