@@ -101,6 +101,8 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
   uint64_t thr[MQ];
 #pragma unroll
   for (int a = 0; a < MQ; ++a) thr[a] = kEmptyKey;
+  constexpr int kLimit = kBuf - kTile;  // a tile appends at most kTile keys to a query's buffer
+  bool over = false;                    // one of this thread's appends landed above kLimit
 
   // with two buffers the copy of tile t+1 runs while tile t is scored; with one (large d)
   // each tile is copied, then scored
@@ -170,12 +172,22 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
       for (int b = 0; b < 4; ++b) {
         if (pbase + b >= n) continue;
         float dist = finish_distance<DIST>(acc[a][b], acc2[a][b], qn[qi], xn[b]);
-        topc_push(S, qi, make_key(dist, (int)(pbase + b)), thr[a]);
+        const uint64_t key = make_key(dist, (int)(pbase + b));
+        if (key < thr[a]) {
+          const int pos = atomicAdd(&S.cnt[qi], 1);
+          S.buf[(size_t)qi * kBuf + pos] = key;
+          over |= pos >= kLimit;
+        }
       }
     }
-    topc_flush(S, QB, kBuf - kTile);
+    // one barrier a tile: every read of this tile's buffer is done (the next copy may
+    // reuse it) and, only if some buffer passed kLimit, the buffers are folded
+    if (__syncthreads_or(over)) {
+      topc_flush(S, QB, kLimit);
 #pragma unroll
-    for (int a = 0; a < MQ; ++a) thr[a] = S.thr[tq * MQ + a];
+      for (int a = 0; a < MQ; ++a) thr[a] = S.thr[tq * MQ + a];
+    }
+    over = false;
   }
   topc_flush(S, QB, 0);
 
