@@ -336,11 +336,14 @@ def main():
     stream = torch.cuda.Stream(device=dev)
     sh = stream.cuda_stream
 
+    # batches are enqueued back to back on one stream (lshg_index_query_async); the timed
+    # region ends with lshg_index_sync, which also reports any device-side error
     def step():
-        idx.query_device(qd.data_ptr(), N_QUERY, K, out.data_ptr(), stream=sh)
+        idx.query_device_async(qd.data_ptr(), N_QUERY, K, out.data_ptr(), stream=sh)
 
     for _ in range(args.warmup):
         step()
+    idx.sync(sh)
     torch.cuda.synchronize()
 
     def barrier():
@@ -359,6 +362,7 @@ def main():
         for _ in range(args.steps):
             step()
         e1.record(stream)
+        idx.sync(sh)
         barrier()
     L.profile_enable(False)
     launches = L.launch_count() - launches0

@@ -207,6 +207,14 @@ class Index:
         """Queries and results already in device memory (float [nq][d], Point [nq][k])."""
         check(lib().lshg_index_query(self._h, q_ptr, nq, k, out_ptr, 1, stream))
 
+    def query_device_async(self, q_ptr: int, nq: int, k: int, out_ptr: int, stream: int | None = None) -> None:
+        """Enqueue a batch (device buffers) without waiting; see `sync`."""
+        check(lib().lshg_index_query_async(self._h, q_ptr, nq, k, out_ptr, stream))
+
+    def sync(self, stream: int | None = None) -> None:
+        """Wait for enqueued batches and raise the first device error kept since the last report."""
+        check(lib().lshg_index_sync(self._h, stream))
+
     def export(self, what: int) -> bytes:
         nb = C.c_size_t(0)
         check(lib().lshg_index_export(self._h, what, None, C.byref(nb)))

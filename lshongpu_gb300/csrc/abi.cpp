@@ -273,6 +273,29 @@ int lshg_index_query(lshg_index* idx, const float* queries, int N_query, int k, 
   });
 }
 
+int lshg_index_query_async(lshg_index* idx, const float* d_queries, int N_query, int k, lshg_point* d_results,
+                           void* stream) {
+  return guarded([&] {
+    LSHG_REQUIRE(idx && d_results && (d_queries || N_query == 0), "NULL argument");
+    Index& I = *idx->impl;
+    cudaStream_t s = stream ? (cudaStream_t)stream : I.stream;
+    // the pipelines preprocess queries in place: work on a stream-ordered copy
+    DevBuf<float> q((size_t)N_query * I.d, s);
+    if (N_query) LSHG_CUDA(cudaMemcpyAsync(q.ptr, d_queries, q.bytes(), cudaMemcpyDeviceToDevice, s));
+    query_index(I, q.ptr, N_query, k, d_results, s);
+  });
+}
+
+int lshg_index_sync(lshg_index* idx, void* stream) {
+  return guarded([&] {
+    LSHG_REQUIRE(idx, "NULL argument");
+    Index& I = *idx->impl;
+    cudaStream_t s = stream ? (cudaStream_t)stream : I.stream;
+    LSHG_CUDA(cudaStreamSynchronize(s));
+    query_error(I, s);
+  });
+}
+
 int lshg_index_free(lshg_index* idx) {
   return guarded([&] { delete idx; });
 }

@@ -155,4 +155,37 @@ __device__ __forceinline__ void topc_flush(TopCShared s, int nq, int limit) {
   __syncthreads();
 }
 
+// Warp-wide bitonic network on 32*E 64-bit keys held as x[e] of lane l = element e*32+l.
+// Sorts ascending when `merge_only` is false; with `merge_only` the input must already
+// be bitonic and one merge pass sorts it.
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint64_t (&x)[E], int lane, bool merge_only) {
+  constexpr int N = 32 * E;
+#pragma unroll
+  for (int k = 2; k <= N; k <<= 1) {
+    if (merge_only && k != N) continue;
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int i = e * 32 + lane;
+        const bool up = (i & k) == 0 || merge_only;
+        if (j >= 32) {
+          const int f = e ^ (j >> 5);
+          if (f > e) {  // both elements live in this lane
+            const uint64_t lo = x[e] < x[f] ? x[e] : x[f];
+            const uint64_t hi = x[e] < x[f] ? x[f] : x[e];
+            x[e] = up ? lo : hi;
+            x[f] = up ? hi : lo;
+          }
+        } else {
+          const uint64_t o = __shfl_xor_sync(0xffffffffu, x[e], j);
+          const bool lower = (lane & j) == 0;
+          x[e] = (lower == up) ? (x[e] < o ? x[e] : o) : (x[e] < o ? o : x[e]);
+        }
+      }
+    }
+  }
+}
+
 }  // namespace lshg

@@ -1,0 +1,53 @@
+"""The stream-ordered query entry point (lshg_index_query_async + lshg_index_sync): the
+same results as the synchronous query, several batches in flight on one stream, and
+device-side errors kept until the next synchronisation reports them."""
+import numpy as np
+import pytest
+
+from lshongpu_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+
+D = 100
+
+
+@pytest.mark.parametrize("impl", ["tc", "exact"])
+def test_async_batches_match_sync_query(engine, impl):
+    import torch
+
+    x = datasets.clustered(30000, D, 141, count=40)
+    qs = [datasets.clustered(257, D, 142 + i, count=40) for i in range(3)]
+    code = engine.IMPL_TC if impl == "tc" else engine.IMPL_EXACT
+    idx = engine.Index(x, implementation=code, distanceFunc=1)
+    refs = [idx.query(q, 32) for q in qs]
+    stream = torch.cuda.Stream()
+    dqs = [torch.from_numpy(q).cuda() for q in qs]
+    outs = [torch.full((q.shape[0], 32, 2), -7, dtype=torch.int32, device="cuda") for q in qs]
+    torch.cuda.synchronize()
+    for dq, out in zip(dqs, outs):  # three batches in flight, no host wait in between
+        idx.query_device_async(dq.data_ptr(), dq.shape[0], 32, out.data_ptr(), stream=stream.cuda_stream)
+    idx.sync(stream.cuda_stream)
+    for dq, q, out, ref in zip(dqs, qs, outs, refs):
+        got = out.cpu().numpy()
+        assert np.array_equal(got[:, :, 0], ref["ID"])
+        assert np.array_equal(got[:, :, 1].view(np.float32), ref["distance"])
+        assert np.array_equal(dq.cpu().numpy(), q)  # the caller's queries are untouched
+
+
+def test_async_device_error_reported_at_sync(engine):
+    """A zero query row makes the weighted-MinHash sampler hit its draw limit on the
+    device; the asynchronous call returns at once and the next sync reports it."""
+    import torch
+
+    x = datasets.sparse_gamma(2000, D, 151)
+    q = datasets.sparse_gamma(8, D, 152)
+    q[3] = 0.0
+    idx = engine.Index(x, implementation=4, distanceFunc=2, sketchDim=64)
+    dq = torch.from_numpy(q).cuda()
+    out = torch.empty((8, 32, 2), dtype=torch.int32, device="cuda")
+    idx.query_device_async(dq.data_ptr(), 8, 32, out.data_ptr())
+    with pytest.raises(engine.LshgError) as e:
+        idx.sync()
+    assert e.value.status == 6  # LSHG_ERR_SAMPLER_LIMIT
+    idx.sync()  # the error was reported once; the index stays usable
+    assert idx.query(q[:3], 32).shape == (3, 32)
