@@ -9,9 +9,10 @@
 //     of them, tau[q] (tau_select_kernel), is a lower bound of the query's true CT-th best
 //     score: every point of the exact top-CT has score >= tau[q].
 //   pass 1 (MODE_FILTER) runs on the whole base.  The epilogue compares each score with
-//     its row's tau and appends the (rare) survivors to the query's candidate array in
-//     global memory with one atomicAdd each; there is no per-row state on chip, so the
-//     epilogue is a 64-wide maximum and a warp vote per tile in the common case.
+//     its row's tau; the (rare) survivors are staged per row in shared memory and moved
+//     to the query's candidate array in global memory with one atomicAdd a batch (at the
+//     end of each work unit, or when the 8-entry staging is full).  There is no per-row
+//     selection state on chip, so the common case is a 64-wide maximum and a warp vote.
 //
 // cand_select_kernel then sorts each query's survivors and keeps the first CT keys
 // (score descending, ties by lower id) -- exactly the top-CT by tensor-core score.  A query
