@@ -156,6 +156,8 @@ def build_index(L, x, path: str):
 
 # FP32 SIMT peak (no measured figure exists for it): 152 SMs x 128 FMA/clk x 2 x 2.07 GHz
 FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+# 32-bit population count: 16 a clock an SM (nominal), 152 SMs at 2.07 GHz, in G word/s
+POPC_NOMINAL_GWORDS = 152 * 16 * 2.07e9 / 1e9
 
 
 def algorithmic(path: str, prof: dict, nq: int):
@@ -168,12 +170,14 @@ def algorithmic(path: str, prof: dict, nq: int):
         return "tc_filter", "tensor", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
     if path == "exact":
         return "scan_float", "fp32", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
+    # sketch scans are integer-bound at these batch sizes: work = sketch words compared
+    # (one XOR + POPC each, zero-byte count for byte samples), Q x N x words
     if path == "simhash":
-        return "scan_bits", "hbm", N_BASE * 128 / 1e9, "GB/s"
+        return "scan_bits", "popc", nq * N_BASE * 32 / 1e9, "Gword/s"
     if path == "wmh":
-        return "scan_bits", "hbm", N_BASE * 256 / 1e9, "GB/s"
+        return "scan_bits", "popc", nq * N_BASE * 64 / 1e9, "Gword/s"
     if path == "wmh1":
-        return "scan_bits", "hbm", N_BASE * 32 / 1e9, "GB/s"
+        return "scan_bits", "popc", nq * N_BASE * 8 / 1e9, "Gword/s"
     return "lsh_query", "gather", None, None
 
 
@@ -402,6 +406,8 @@ def main():
         peak, peak_kind = FP32_SIMT_NOMINAL_TFLOPS, "nominal (152 SMs x 128 FMA/clk x 2 x 2.07 GHz)"
     elif bound == "tensor":
         peak = bf16
+    elif bound == "popc":
+        peak, peak_kind = POPC_NOMINAL_GWORDS, "nominal (152 SMs x 16 popc/clk x 2.07 GHz)"
     else:
         peak = None
     # DRAM bytes of one tc_filter launch at the headline shape, from the committed ncu
