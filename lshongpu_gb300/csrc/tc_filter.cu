@@ -78,6 +78,7 @@ struct FilterArgs {
   uint64_t* cand;    // [nq][cap] survivor keys
   int cap;
   int ksteps;    // K=16 MMA steps covering the data dimension
+  int hi_cols;   // columns loaded of the second 64-column half of a base tile
   int* err;
 };
 
@@ -96,7 +97,7 @@ __device__ __forceinline__ void flush_staged(int* cnt, uint64_t* dst, int cap, c
 template <int MODE, int GW>
 __global__ void __launch_bounds__(F_THREADS, 1)
     tc_filter_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                     const FilterArgs a) {
+                     const __grid_constant__ CUtensorMap mapBhi, const FilterArgs a) {
   static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column pieces");
   static_assert(GW == 64 || GW == 8, "group width");
   const int U = a.NCH * a.QT;
@@ -160,9 +161,9 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
           const uint32_t dst = s0 + F_B_OFF + st * B_TILE;
           const int row = p * a.dstride * TN;
-          mbar_expect_tx(FULL(st), B_TILE);
+          mbar_expect_tx(FULL(st), B_HALF + TN * a.hi_cols * 2);
           tma_load_2d(dst, &mapB, 0, row, FULL(st));
-          tma_load_2d(dst + B_HALF, &mapB, KHALF, row, FULL(st));
+          tma_load_2d(dst + B_HALF, &mapBhi, KHALF, row, FULL(st));
           ++it;
         }
       }
@@ -459,7 +460,8 @@ __global__ void merge_fallback_kernel(const uint64_t* __restrict__ part, const i
 }
 
 template <int MODE, int GW>
-void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, FilterArgs a, const char* name, cudaStream_t s) {
+void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, FilterArgs a, const char* name,
+                cudaStream_t s) {
   // chunk size: long enough to amortise the query-tile switch, short enough for >= 4
   // units per CTA
   const int G = num_sms();
@@ -471,7 +473,7 @@ void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, FilterArgs a, cons
   auto kern = tc_filter_kernel<MODE, GW>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM));
   ProfScope _ps(name, s);
-  kern<<<grid, F_THREADS, F_SMEM, s>>>(ma, mb, a);
+  kern<<<grid, F_THREADS, F_SMEM, s>>>(ma, mb, mbhi, a);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
@@ -508,9 +510,11 @@ FilterPlan plan_filter(int64_t n, int CT) {
   return p;
 }
 
-void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const FilterPlan& plan, int nq, int64_t n,
-                        int d, int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s) {
+void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, int hi_cols,
+                        const FilterPlan& plan, int nq, int64_t n, int d, int QT, int CT, float* tau, int* cnt,
+                        uint64_t* cand, int* err, cudaStream_t s) {
   FilterArgs a{};
+  a.hi_cols = hi_cols;
   a.nq = nq;
   a.ksteps = tc_ksteps(d);
   a.n = n;
@@ -522,8 +526,8 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const Filt
     a.dstride = plan.S;
     a.gmax = gmax.ptr;
     a.M = plan.M;
-    if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64>(ma, mb, a, "tc_prepass", s);
-    else run_filter<MODE_GROUPMAX, 8>(ma, mb, a, "tc_prepass", s);
+    if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64>(ma, mb, mbhi, a, "tc_prepass", s);
+    else run_filter<MODE_GROUPMAX, 8>(ma, mb, mbhi, a, "tc_prepass", s);
     {
       ProfScope _ps("tc_tau_select", s);
       tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, kTauMargin, tau);
@@ -539,7 +543,7 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const Filt
   a.cnt = cnt;
   a.cand = cand;
   a.cap = plan.cap;
-  run_filter<MODE_FILTER, 64>(ma, mb, a, "tc_filter", s);
+  run_filter<MODE_FILTER, 64>(ma, mb, mbhi, a, "tc_filter", s);
 }
 
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,

@@ -30,8 +30,10 @@ struct FilterPlan {
 FilterPlan plan_filter(int64_t n, int CT);
 
 // Prepass + threshold selection + filter pass: fills cnt[q] and cand[q][0..cap).
-void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const FilterPlan& plan, int nq, int64_t n,
-                        int d, int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s);
+// mb: base tiles (256 rows x 64 columns boxes); mbhi: boxes of the second 64-column half
+// trimmed to hi_cols columns (the K steps past the data dimension are never read).
+void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, int hi_cols,
+                        const FilterPlan& plan, int nq, int64_t n, int d, int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s);
 
 // Top-CT keys a query from its survivors; overflowed queries are listed in ovf.
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,

@@ -172,7 +172,7 @@ __device__ __forceinline__ float max8(const uint32_t (&v)[64], int g) {
 
 // Tensor map over `rows` bf16 rows of KD elements; boxes of 64 columns x box_rows rows
 // with 128-byte swizzle (the layout smem_desc describes).
-CUtensorMap make_map(const void* base, int64_t rows, int box_rows = BM);
+CUtensorMap make_map(const void* base, int64_t rows, int box_rows = BM, int box_cols = KHALF);
 
 }  // namespace tc
 }  // namespace lshg

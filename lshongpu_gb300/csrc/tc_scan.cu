@@ -412,14 +412,16 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// Rows of KD bf16 (256 B); boxes of 64 columns x 128 rows with 128-byte swizzle.
-CUtensorMap make_map(const void* base, int64_t rows, int box_rows) {
+// Rows of KD bf16 (256 B); boxes of box_cols (<= 64) columns x box_rows rows with 128-byte
+// swizzle.
+CUtensorMap make_map(const void* base, int64_t rows, int box_rows, int box_cols) {
   LSHG_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
   CUtensorMap m;
   cuuint64_t dims[2] = {(cuuint64_t)KD, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)KD * 2};
   LSHG_REQUIRE(box_rows >= 1 && box_rows <= 256, "TMA box rows must be in [1, 256]");
-  cuuint32_t box[2] = {(cuuint32_t)KHALF, (cuuint32_t)box_rows};
+  LSHG_REQUIRE(box_cols >= 8 && box_cols <= KHALF && box_cols % 8 == 0, "TMA box columns must be 8..64, multiple of 8");
+  cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -475,6 +477,9 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   const int64_t npad = (int64_t)ceil_div(I.n, FILTER_TN) * FILTER_TN;
   const CUtensorMap mb = make_map(I.xbf.ptr, npad);                    // list kernel: 128-row boxes
   const CUtensorMap mb256 = make_map(I.xbf.ptr, npad, FILTER_TN);      // filter: 256-row boxes
+  // the filter's second 64-column half only up to the last K step (columns 64..16*ksteps)
+  const int hi_cols = std::max(8, std::min(KHALF, 16 * tc_ksteps(I.d) - KHALF));
+  const CUtensorMap mb256hi = make_map(I.xbf.ptr, npad, FILTER_TN, hi_cols);
 
   // 1-2. thresholds and survivors
   DevBuf<float> tau((size_t)nq, s);
@@ -482,7 +487,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   int* ovf = cnt.ptr + nq;
   LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, (size_t)(nq + 1) * sizeof(int), s));
   DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
-  launch_filter_scan(ma, mb256, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
+  launch_filter_scan(ma, mb256, mb256hi, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
 
   // 3. top-CT of the survivors
   DevBuf<uint64_t> best((size_t)nq * CT, s);
