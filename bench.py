@@ -333,7 +333,9 @@ def main():
     import lshongpu_gb300 as L
 
     x, q = make_data(rank)
+    tb = time.perf_counter()
     idx = build_index(L, x, args.path)
+    build_s = time.perf_counter() - tb  # host wall time of the index build (synchronous)
     dev = torch.device("cuda", local)
     qd = torch.from_numpy(q).to(dev)
     out = torch.empty((N_QUERY, K, 2), dtype=torch.int32, device=dev)
@@ -486,6 +488,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERY * (DIM + PAD_DIM) * 4,
                 "d2h_bytes_per_step": N_QUERY * K * 8},
         "gpu_launches": launches,
+        "index_build_s": build_s,
         "clocks": clk.summary(),
         "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
     }
