@@ -462,11 +462,11 @@ __global__ void merge_fallback_kernel(const uint64_t* __restrict__ part, const i
 template <int MODE, int GW>
 void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, FilterArgs a, const char* name,
                 cudaStream_t s) {
-  // chunk size: long enough to amortise the query-tile switch, short enough for >= 4
-  // units per CTA
+  // chunk size: long enough to amortise the query-tile switch (at most 32 tiles), short
+  // enough for >= 16 units per CTA so the last unit leaves little imbalance
   const int G = num_sms();
   const int64_t work = (int64_t)a.NP * a.QT;
-  a.CH = (int)std::max<int64_t>(1, std::min<int64_t>(32, (work + 4 * G - 1) / (4 * G)));
+  a.CH = (int)std::max<int64_t>(1, std::min<int64_t>(32, (work + 16 * G - 1) / (16 * G)));
   a.NCH = ceil_div(a.NP, a.CH);
   const int U = a.NCH * a.QT;
   const int grid = std::min(G, U);
