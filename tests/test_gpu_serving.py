@@ -21,7 +21,8 @@ def indexes(engine):
     sim = engine.Index(x, implementation=3, sketchDim=16, options=engine.make_options(candidates=256))
     cp = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=16,
                       tables=8, options=engine.make_options(cp_hashes=2))
-    return x, {0: exact, 1: sim, 2: cp}
+    tc = engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=1)
+    return x, {0: exact, 1: sim, 2: cp, 3: tc}
 
 
 def test_same_alone_and_in_the_mix(engine, indexes):
@@ -32,7 +33,7 @@ def test_same_alone_and_in_the_mix(engine, indexes):
         srv.add_index(i, ix)
     reqs = []
     for t in range(60):
-        which = int(rng.integers(0, 3))
+        which = int(rng.integers(0, len(idx)))
         nq = int(np.exp(rng.uniform(0, np.log(300))))
         k = int(rng.choice([10, 32, 100]))
         q = datasets.clustered(nq, D, 1000 + t, count=50)
