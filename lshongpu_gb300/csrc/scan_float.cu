@@ -197,6 +197,216 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Register-blocked variant for C <= 128 (k <= 128): 64 queries a CTA, warp w owns
+// queries 8w .. 8w+7 and lane l points 4l .. 4l+3 of each 128-point tile, so a thread
+// keeps an 8 x 4 micro-tile (32 FMAs per dimension step for three shared loads).  A
+// query's top-C list lives in shared memory and is touched only when some candidate of
+// the tile beats the query's threshold (one warp vote); there is no block-level selection
+// protocol and no barrier besides the tile copy's.
+// ---------------------------------------------------------------------------------
+constexpr int kRegQB = 64;
+
+__host__ __device__ inline size_t reg_scan_smem(int d, int C, int nbuf) {
+  size_t off = 0;
+  smem_take(off, (size_t)nbuf * kTile * d * 4);  // point tiles
+  smem_take(off, (size_t)kRegQB * d * 4);        // queries, [j][64]
+  smem_take(off, (size_t)kRegQB * 4);            // query magnitudes
+  smem_take(off, (size_t)kRegQB * C * 8);        // top-C lists
+  smem_take(off, (size_t)8 * 32 * 8);            // per-warp scratch
+  return off;
+}
+
+// Merge one query's candidates (k0..k3 on every lane: 128 keys, only those below `thr`
+// count) into its sorted list of C = 32*EC keys in shared memory; returns the new
+// threshold (the list's last key).  Few survivors are compacted to one key a lane and
+// sorted; more than 32 sort all 128.  Executed by the whole warp; kept out of line
+// because it runs rarely.
+template <int EC>
+__device__ __noinline__ uint64_t merge_candidates(uint64_t* list, uint64_t k0, uint64_t k1, uint64_t k2,
+                                                  uint64_t k3, uint64_t thr, uint64_t* scratch) {
+  const int lane = threadIdx.x & 31;
+  const int cnt = (k0 < thr) + (k1 < thr) + (k2 < thr) + (k3 < thr);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  uint64_t x[EC];
+  if (total <= 32) {
+    int pos = incl - cnt;
+    if (k0 < thr) scratch[pos++] = k0;
+    if (k1 < thr) scratch[pos++] = k1;
+    if (k2 < thr) scratch[pos++] = k2;
+    if (k3 < thr) scratch[pos++] = k3;
+    __syncwarp();
+    x[0] = lane < total ? scratch[lane] : kEmptyKey;
+#pragma unroll
+    for (int e = 1; e < EC; ++e) x[e] = kEmptyKey;
+    __syncwarp();
+    warp_bitonic<EC>(x, lane, false);
+  } else {
+    uint64_t y[4] = {k0 < thr ? k0 : kEmptyKey, k1 < thr ? k1 : kEmptyKey, k2 < thr ? k2 : kEmptyKey,
+                     k3 < thr ? k3 : kEmptyKey};
+    warp_bitonic<4>(y, lane, false);
+#pragma unroll
+    for (int e = 0; e < EC; ++e) x[e] = y[e];  // the 32*EC smallest candidates, ascending
+  }
+  uint64_t best[EC];
+#pragma unroll
+  for (int e = 0; e < EC; ++e) best[e] = list[e * 32 + lane];
+  // best ascending, x ascending: min(best[i], x[C-1-i]) is bitonic and holds the C smallest
+#pragma unroll
+  for (int e = 0; e < EC; ++e) {
+    const uint64_t r = __shfl_sync(0xffffffffu, x[EC - 1 - e], 31 - lane);
+    best[e] = best[e] < r ? best[e] : r;
+  }
+  warp_bitonic<EC>(best, lane, true);
+#pragma unroll
+  for (int e = 0; e < EC; ++e) list[e * 32 + lane] = best[e];
+  return __shfl_sync(0xffffffffu, best[EC - 1], 31);
+}
+
+template <int DIST, int EC>
+__global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
+    const float* __restrict__ xt, int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
+    int nq, const float* __restrict__ qnorm, int tiles_per_split, int splits, int nbuf, uint64_t* __restrict__ out) {
+  constexpr int C = 32 * EC;
+  extern __shared__ __align__(16) unsigned char smem[];
+  size_t off = 0;
+  float* xs = reinterpret_cast<float*>(smem + smem_take(off, (size_t)nbuf * kTile * d * 4));
+  float* qs = reinterpret_cast<float*>(smem + smem_take(off, (size_t)kRegQB * d * 4));
+  float* qn = reinterpret_cast<float*>(smem + smem_take(off, (size_t)kRegQB * 4));
+  uint64_t* lists = reinterpret_cast<uint64_t*>(smem + smem_take(off, (size_t)kRegQB * C * 8));
+  uint64_t* scratch = reinterpret_cast<uint64_t*>(smem + smem_take(off, (size_t)8 * 32 * 8));
+
+  const int q0 = blockIdx.x * kRegQB;
+  const int split = blockIdx.y;
+  const int ntiles = (int)((n + kTile - 1) / kTile);
+  const int t_begin = split * tiles_per_split;
+  const int t_end = min(ntiles, t_begin + tiles_per_split);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  for (int i = threadIdx.x; i < kRegQB * d; i += blockDim.x) {
+    const int qi = i / d, j = i - qi * d;
+    qs[j * kRegQB + qi] = (q0 + qi < nq) ? q[(int64_t)(q0 + qi) * d + j] : 0.0f;
+  }
+  for (int qi = threadIdx.x; qi < kRegQB; qi += blockDim.x)
+    qn[qi] = (DIST == DIST_ANGULAR && q0 + qi < nq) ? qnorm[q0 + qi] : 1.0f;
+  for (int i = threadIdx.x; i < kRegQB * C; i += blockDim.x) lists[i] = kEmptyKey;
+  __syncthreads();  // lists are read by their owning warps (and written out even for an empty split)
+  uint64_t thr[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) thr[a] = kEmptyKey;
+
+  const int tile_f4 = kTile * d / 4;
+  auto slot = [&](int tile) { return nbuf == 2 ? (tile & 1) : 0; };
+  auto issue_tile = [&](int tile) {
+    const float4* src = reinterpret_cast<const float4*>(xt + (int64_t)tile * kTile * d);
+    float4* dst = reinterpret_cast<float4*>(xs) + (size_t)slot(tile) * tile_f4;
+    for (int i = threadIdx.x; i < tile_f4; i += blockDim.x) cp_async16(dst + i, src + i);
+    cp_async_commit();
+  };
+  if (t_begin < t_end) issue_tile(t_begin);
+  for (int tile = t_begin; tile < t_end; ++tile) {
+    if (nbuf == 2 && tile + 1 < t_end) {
+      issue_tile(tile + 1);  // its buffer was last read by tile - 1, finished at the barrier below
+      cp_async_wait<1>();
+    } else {
+      if (nbuf == 1 && tile > t_begin) issue_tile(tile);
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const float* xcur = xs + (size_t)slot(tile) * kTile * d;
+
+    float acc[8][4], acc2[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) { acc[a][b] = 0.0f; acc2[a][b] = 0.0f; }
+    for (int j = 0; j < d; ++j) {
+      const float4 xv = *reinterpret_cast<const float4*>(&xcur[j * kTile + 4 * lane]);
+      const float4 qa0 = *reinterpret_cast<const float4*>(&qs[j * kRegQB + 8 * w]);
+      const float4 qa1 = *reinterpret_cast<const float4*>(&qs[j * kRegQB + 8 * w + 4]);
+      const float xb[4] = {xv.x, xv.y, xv.z, xv.w};
+      const float qv[8] = {qa0.x, qa0.y, qa0.z, qa0.w, qa1.x, qa1.y, qa1.z, qa1.w};
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          if (DIST == DIST_ANGULAR) {
+            acc[a][b] = __fmaf_rn(qv[a], xb[b], acc[a][b]);
+          } else if (DIST == DIST_JACCARD) {
+            acc[a][b] = __fadd_rn(acc[a][b], fminf(xb[b], qv[a]));
+            acc2[a][b] = __fadd_rn(acc2[a][b], fmaxf(xb[b], qv[a]));
+          } else {
+            const float df = __fsub_rn(qv[a], xb[b]);
+            acc[a][b] = __fmaf_rn(df, df, acc[a][b]);
+          }
+        }
+    }
+    const int64_t pbase = (int64_t)tile * kTile + 4 * lane;
+    float xn[4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) xn[b] = (DIST == DIST_ANGULAR && pbase + b < n) ? xnorm[pbase + b] : 1.0f;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int qi = 8 * w + a;
+      if (q0 + qi >= nq) continue;  // warp-uniform
+      uint64_t k[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        k[b] = (pbase + b < n) ? make_key(finish_distance<DIST>(acc[a][b], acc2[a][b], qn[qi], xn[b]), (int)(pbase + b))
+                               : kEmptyKey;
+      if (__any_sync(0xffffffffu, k[0] < thr[a] || k[1] < thr[a] || k[2] < thr[a] || k[3] < thr[a]))
+        thr[a] = merge_candidates<EC>(lists + (size_t)qi * C, k[0], k[1], k[2], k[3], thr[a], scratch + w * 32);
+    }
+    __syncthreads();  // every read of this tile's buffer is done: the next copy may reuse it
+  }
+
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const int qi = 8 * w + a;
+    if (q0 + qi >= nq) continue;
+#pragma unroll
+    for (int e = 0; e < EC; ++e)
+      out[((int64_t)(q0 + qi) * splits + split) * C + e * 32 + lane] = lists[(size_t)qi * C + e * 32 + lane];
+  }
+}
+
+template <int DIST, int EC>
+void launch_reg(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq, const float* qnorm,
+                int splits, int nbuf, uint64_t* out, cudaStream_t s) {
+  ProfScope _ps("scan_float", s);
+  const size_t smem = reg_scan_smem(d, 32 * EC, nbuf);
+  auto kern = scan_float_reg_kernel<DIST, EC>;
+  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int ntiles = ceil_div(n, kTile);
+  const int tps = ceil_div(ntiles, splits);
+  dim3 grid(ceil_div(nq, kRegQB), splits);
+  kern<<<grid, 256, smem, s>>>(xt, n, d, xnorm, q, nq, qnorm, tps, splits, nbuf, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+// The register-blocked kernel serves C <= 128 when its shared memory fits; returns false
+// otherwise (the general kernel runs).
+template <int DIST>
+bool try_launch_reg(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq,
+                    const float* qnorm, int C, int splits, uint64_t* out, cudaStream_t s) {
+  if (C > 128) return false;
+  const size_t cap = 220 * 1024;
+  int nbuf = reg_scan_smem(d, C, 2) <= cap ? 2 : (reg_scan_smem(d, C, 1) <= cap ? 1 : 0);
+  if (!nbuf) return false;
+  if (C == 32) launch_reg<DIST, 1>(xt, n, d, xnorm, q, nq, qnorm, splits, nbuf, out, s);
+  else if (C == 64) launch_reg<DIST, 2>(xt, n, d, xnorm, q, nq, qnorm, splits, nbuf, out, s);
+  else if (C == 128) launch_reg<DIST, 4>(xt, n, d, xnorm, q, nq, qnorm, splits, nbuf, out, s);
+  else return false;
+  return true;
+}
+
 struct FloatCfg {
   int QB, MQ, nbuf;
 };
@@ -229,6 +439,7 @@ void launch_cfg(const float* xt, int64_t n, int d, const float* xnorm, const flo
 template <int DIST>
 void launch_dist(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq, const float* qnorm,
                  int C, int splits, uint64_t* out, cudaStream_t s) {
+  if (try_launch_reg<DIST>(xt, n, d, xnorm, q, nq, qnorm, C, splits, out, s)) return;
   FloatCfg c = pick_float_cfg(d, C);
   if (c.QB == 32) launch_cfg<DIST, 32, 4>(xt, n, d, xnorm, q, nq, qnorm, C, splits, c.nbuf, out, s);
   else if (c.QB == 8) launch_cfg<DIST, 8, 1>(xt, n, d, xnorm, q, nq, qnorm, C, splits, c.nbuf, out, s);
@@ -238,12 +449,26 @@ void launch_dist(const float* xt, int64_t n, int d, const float* xnorm, const fl
 }  // namespace
 
 int scan_float_splits(int64_t n, int nq, int C) {
-  int QB = C <= 128 ? 32 : (C <= 1024 ? 8 : 2);
-  int qblocks = ceil_div(nq, QB);
-  int ntiles = ceil_div(n, kTile);
-  int want = ceil_div((int64_t)num_sms() * 2, qblocks);
-  int maxs = std::max(1, ntiles / 4);
-  return std::max(1, std::min(std::min(want, maxs), 64));
+  // C <= 128 runs the register-blocked kernel (one 64-query CTA an SM), larger C the
+  // general one (two CTAs an SM); pick the split count whose grid fills whole waves best
+  // among those giving at least ~2 CTAs an SM slot, at most 4x that and 64
+  const int QB = C <= 128 ? kRegQB : (C <= 1024 ? 8 : 2);
+  const int slots = num_sms() * (C <= 128 ? 1 : 2);
+  const int qblocks = ceil_div(nq, QB);
+  const int ntiles = ceil_div(n, kTile);
+  const int maxs = std::max(1, std::min(ntiles / 4, 64));
+  const int want = std::max(1, std::min(maxs, ceil_div((int64_t)slots * 2, qblocks)));
+  int best = want;
+  double best_eff = 0.0;
+  for (int sp = want; sp <= std::min(maxs, 4 * want); ++sp) {
+    const int64_t ctas = (int64_t)qblocks * sp;
+    const double eff = (double)ctas / (double)(ceil_div(ctas, slots) * (int64_t)slots);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = sp;
+    }
+  }
+  return best;
 }
 
 int launch_scan_float(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq,
