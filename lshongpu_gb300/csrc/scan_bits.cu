@@ -197,12 +197,27 @@ void launch_width(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, 
 }  // namespace
 
 int scan_bits_splits(int64_t n, int nq, int C) {
-  int QB = C <= 128 ? 32 : (C <= 1024 ? 8 : 2);
-  int qblocks = ceil_div(nq, QB);
-  int ntiles = ceil_div(n, kTile);
-  int want = ceil_div((int64_t)num_sms() * 3, qblocks);
-  int maxs = std::max(1, ntiles / 4);
-  return std::max(1, std::min(std::min(want, maxs), 64));
+  // two CTAs an SM; for C <= 128 pick the split count whose grid fills whole waves best,
+  // between the count giving ~1.5 CTAs a slot and 4x that (at most 64 splits, >= 4 tiles
+  // a split)
+  const int QB = C <= 128 ? 32 : (C <= 1024 ? 8 : 2);
+  const int slots = num_sms() * 2;
+  const int qblocks = ceil_div(nq, QB);
+  const int ntiles = ceil_div(n, kTile);
+  const int maxs = std::max(1, std::min(ntiles / 4, 64));
+  const int want = std::max(1, std::min(maxs, ceil_div((int64_t)num_sms() * 3, qblocks)));
+  if (C > 128) return want;  // large lists: every extra split restarts them cold, which costs more than the tail
+  int best = want;
+  double best_eff = 0.0;
+  for (int sp = want; sp <= std::min(maxs, 4 * want); ++sp) {
+    const int64_t ctas = (int64_t)qblocks * sp;
+    const double eff = (double)ctas / (double)(ceil_div(ctas, slots) * (int64_t)slots);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = sp;
+    }
+  }
+  return best;
 }
 
 int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int op,
