@@ -149,14 +149,17 @@ int lshg_index_query(lshg_index* idx, const float* queries, int N_query, int k, 
                      int on_device, void* stream);
 int lshg_index_free(lshg_index* idx);
 /* Stream-ordered query (no counterpart in the reference, which answers one synchronous
- * batch per run).  d_queries [N_query][d] and d_results [N_query][k] are device
- * pointers; the batch is enqueued on `stream` (NULL = index stream) and the call returns
- * without waiting, so a caller can keep several batches in flight.  Argument errors are
- * returned at once; errors found on the device (a pipeline wait timed out, the MinHash
- * sampler limit) are kept and reported by the next lshg_index_sync or lshg_index_query
- * on the index.  The caller's query buffer is not modified. */
-int lshg_index_query_async(lshg_index* idx, const float* d_queries, int N_query, int k, lshg_point* d_results,
-                           void* stream);
+ * batch per run).  queries [N_query][d] and results [N_query][k] are device pointers
+ * when on_device, else host pointers (page-locked for the copies to run asynchronously;
+ * they must stay valid until the stream is synchronised).  The batch -- host-to-device
+ * copy, query, device-to-host copy -- is enqueued on `stream` (NULL = index stream) and
+ * the call returns without waiting, so a caller can keep several batches in flight on
+ * one or more streams.  Argument errors are returned at once; errors found on the device
+ * (a pipeline wait timed out, the MinHash sampler limit) are kept and reported by the
+ * next lshg_index_sync or lshg_index_query on the index.  The query buffer is not
+ * modified. */
+int lshg_index_query_async(lshg_index* idx, const float* queries, int N_query, int k, lshg_point* results,
+                           int on_device, void* stream);
 /* Wait for every batch enqueued on `stream` (NULL = index stream) and report device
  * errors kept since the last report. */
 int lshg_index_sync(lshg_index* idx, void* stream);

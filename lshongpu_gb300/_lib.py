@@ -93,7 +93,7 @@ _SIGS = {
     "lshg_index_query": (c_int, [P, P, c_int, c_int, P, c_int, P]),
     "lshg_index_free": (c_int, [P]),
     "lshg_index_query_noalloc": (c_int, [P, P, c_int, c_int, P, P]),
-    "lshg_index_query_async": (c_int, [P, P, c_int, c_int, P, P]),
+    "lshg_index_query_async": (c_int, [P, P, c_int, c_int, P, c_int, P]),
     "lshg_index_sync": (c_int, [P, P]),
     "lshg_index_export": (c_int, [P, c_int, P, C.POINTER(c_size_t)]),
     "lshg_index_sketch_queries": (c_int, [P, P, c_int, P, P]),

@@ -209,7 +209,12 @@ class Index:
 
     def query_device_async(self, q_ptr: int, nq: int, k: int, out_ptr: int, stream: int | None = None) -> None:
         """Enqueue a batch (device buffers) without waiting; see `sync`."""
-        check(lib().lshg_index_query_async(self._h, q_ptr, nq, k, out_ptr, stream))
+        check(lib().lshg_index_query_async(self._h, q_ptr, nq, k, out_ptr, 1, stream))
+
+    def query_host_async(self, q_ptr: int, nq: int, k: int, out_ptr: int, stream: int | None = None) -> None:
+        """Enqueue a batch on host (page-locked) buffers -- upload, query, download --
+        without waiting; the buffers must stay valid until `sync`."""
+        check(lib().lshg_index_query_async(self._h, q_ptr, nq, k, out_ptr, 0, stream))
 
     def sync(self, stream: int | None = None) -> None:
         """Wait for enqueued batches and raise the first device error kept since the last report."""

@@ -273,16 +273,25 @@ int lshg_index_query(lshg_index* idx, const float* queries, int N_query, int k, 
   });
 }
 
-int lshg_index_query_async(lshg_index* idx, const float* d_queries, int N_query, int k, lshg_point* d_results,
-                           void* stream) {
+int lshg_index_query_async(lshg_index* idx, const float* queries, int N_query, int k, lshg_point* results,
+                           int on_device, void* stream) {
   return guarded([&] {
-    LSHG_REQUIRE(idx && d_results && (d_queries || N_query == 0), "NULL argument");
+    LSHG_REQUIRE(idx && results && (queries || N_query == 0), "NULL argument");
     Index& I = *idx->impl;
     cudaStream_t s = stream ? (cudaStream_t)stream : I.stream;
     // the pipelines preprocess queries in place: work on a stream-ordered copy
     DevBuf<float> q((size_t)N_query * I.d, s);
-    if (N_query) LSHG_CUDA(cudaMemcpyAsync(q.ptr, d_queries, q.bytes(), cudaMemcpyDeviceToDevice, s));
-    query_index(I, q.ptr, N_query, k, d_results, s);
+    if (N_query)
+      LSHG_CUDA(cudaMemcpyAsync(q.ptr, queries, q.bytes(), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                s));
+    if (on_device) {
+      query_index(I, q.ptr, N_query, k, results, s);
+    } else {
+      DevBuf<lshg_point> out((size_t)N_query * k, s);
+      query_index(I, q.ptr, N_query, k, out.ptr, s);
+      if (N_query)
+        LSHG_CUDA(cudaMemcpyAsync(results, out.ptr, out.bytes(), cudaMemcpyDeviceToHost, s));
+    }
   });
 }
 

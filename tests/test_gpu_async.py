@@ -34,6 +34,35 @@ def test_async_batches_match_sync_query(engine, impl):
         assert np.array_equal(dq.cpu().numpy(), q)  # the caller's queries are untouched
 
 
+@pytest.mark.parametrize("impl", ["tc", "lsh"])
+def test_async_host_buffers_two_streams(engine, impl):
+    """Host (page-locked) buffers: upload, query and download enqueued per batch on two
+    streams at once; every batch equals the synchronous query."""
+    import torch
+
+    x = datasets.clustered(30000, D, 143, count=40)
+    qs = [datasets.clustered(300 + 17 * i, D, 144 + i, count=40) for i in range(4)]
+    if impl == "tc":
+        idx = engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=1)
+    else:
+        idx = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=16,
+                           tables=8, options=engine.make_options(cp_hashes=2))
+    refs = [idx.query(q, 16) for q in qs]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    hqs = [torch.from_numpy(q).pin_memory() for q in qs]
+    outs = [torch.full((q.shape[0], 16, 2), -7, dtype=torch.int32).pin_memory() for q in qs]
+    torch.cuda.synchronize()
+    for i, (hq, out) in enumerate(zip(hqs, outs)):
+        idx.query_host_async(hq.data_ptr(), hq.shape[0], 16, out.data_ptr(), stream=streams[i & 1].cuda_stream)
+    for st in streams:
+        idx.sync(st.cuda_stream)
+    for hq, q, out, ref in zip(hqs, qs, outs, refs):
+        got = out.numpy()
+        assert np.array_equal(got[:, :, 0], ref["ID"])
+        assert np.array_equal(got[:, :, 1].view(np.float32), ref["distance"])
+        assert np.array_equal(hq.numpy(), q)
+
+
 def test_async_device_error_reported_at_sync(engine):
     """A zero query row makes the weighted-MinHash sampler hit its draw limit on the
     device; the asynchronous call returns at once and the next sync reports it."""
