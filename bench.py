@@ -162,7 +162,7 @@ FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 POPC_NOMINAL_GWORDS = 152 * 16 * 2.07e9 / 1e9
 
 
-def algorithmic(path: str, prof: dict, nq: int):
+def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
     """(kernel, bound, work per launch, unit) for the dominant kernel of the path.  FLOPs
     count the index dimension (100 at the headline: the kernel's own padding to 112/128 is
     not counted; 128 at configuration 3, whose vectors carry 28 zero dimensions); sketch
@@ -180,7 +180,15 @@ def algorithmic(path: str, prof: dict, nq: int):
         return "scan_bits", "popc", nq * N_BASE * 64 / 1e9, "Gword/s"
     if path == "wmh1":
         return "scan_bits", "popc", nq * N_BASE * 8 / 1e9, "Gword/s"
-    return "lsh_query", "gather", None, None
+    # LSH gather: bytes the query kernel must move -- every bucket entry walked (4 B id),
+    # every distinct candidate's row and norm, the queries and the results -- from the
+    # kernel's own counters over the timed launches
+    if lsh_counts is None:
+        return "lsh_query", "gather", None, None
+    entries, distinct = lsh_counts
+    dims = d + PAD_DIM
+    return ("lsh_query", "gather",
+            (entries * 4 + distinct * (4 * dims + 4) + nq * (4 * dims + 8 * K)) / 1e9, "GB/s")
 
 
 def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7) -> dict:
@@ -360,6 +368,7 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    counts0 = idx.query_counters()
     launches0 = L.launch_count()
     L.profile_enable(True)
     L.profile_report()
@@ -375,6 +384,7 @@ def main():
     L.profile_enable(False)
     launches = L.launch_count() - launches0
     prof = L.profile_report()
+    counts1 = idx.query_counters()  # the timed launches only (the e2e loop below queries too)
     ms = e0.elapsed_time(e1)
     if dist:
         t = torch.tensor([ms], device=dev)
@@ -422,10 +432,13 @@ def main():
     blocking_value = world * N_QUERY / ((time.perf_counter() - t0) / args.steps)
 
     hbm, bf16, bf16s, peak_kind = peaks()
-    kname, bound, work, unit = algorithmic(args.path, prof, N_QUERY)
+    lsh_counts = None
+    if args.path == "cplsh":
+        lsh_counts = tuple((b - a) / args.steps for a, b in zip(counts0, counts1))
+    kname, bound, work, unit = algorithmic(args.path, prof, N_QUERY, lsh_counts)
     cnt, kms = prof.get(kname, (0, 0.0))
     achieved = (work / (kms / cnt / 1e3)) if (cnt and work) else None
-    if bound == "hbm":
+    if bound in ("hbm", "gather"):
         peak = hbm
     elif bound == "fp32":
         peak, peak_kind = FP32_SIMT_NOMINAL_TFLOPS, "nominal (152 SMs x 128 FMA/clk x 2 x 2.07 GHz)"
@@ -437,7 +450,7 @@ def main():
         peak = None
     # DRAM bytes of one tc_filter launch at the headline shape, from the committed ncu
     # capture (profiles/tc_filter_1.2Mx100_q10k_dram.md): the base once + survivors
-    traffic = 310.21e6 + 36.82e6 if (args.config is None and args.path == "tc" and N_BASE == 1_200_000
+    traffic = 310.19e6 + 36.78e6 if (args.config is None and args.path == "tc" and N_BASE == 1_200_000
                                      and N_QUERY == 10_000) else None
     roofline = {"bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": unit,
                 "frac": (achieved / peak) if (achieved and peak) else None, "peak_source": peak_kind,

@@ -182,6 +182,9 @@ int lshg_index_query_noalloc(lshg_index* idx, const float* d_queries, int N_quer
  *  2 = LSH keys (u16 [n][tables])
  *  3 = LSH bucket offsets (int32 [tables][tableSize], absolute into the bucket array)
  *  4 = LSH bucket ids (int32 [tables][n], ascending ids within each bucket)
+ *  5 = query counters (uint64 [2], cumulative since the build or load: LSH bucket
+ *      entries walked, distinct LSH candidates scored); read after the queries' streams
+ *      have been synchronised
  * If dst is NULL only *bytes is set. */
 int lshg_index_export(lshg_index* idx, int what, void* dst, size_t* bytes);
 /* Hash/sketch queries with the index's random vectors: sketches and keys as in export. */

@@ -227,6 +227,12 @@ class Index:
         check(lib().lshg_index_export(self._h, what, buf, C.byref(nb)))
         return bytes(buf[: nb.value])
 
+    def query_counters(self) -> tuple[int, int]:
+        """(LSH bucket entries walked, distinct LSH candidates scored), cumulative since
+        the build or load; read after the queries' streams have been synchronised."""
+        v = np.frombuffer(self.export(5), dtype=np.uint64)
+        return int(v[0]), int(v[1])
+
     def sketch_queries(self, queries, sketch_dtype, sketch_width: int, tables: int = 0):
         q = _f32(queries)
         nq = q.shape[0]

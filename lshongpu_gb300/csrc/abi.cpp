@@ -326,6 +326,7 @@ int lshg_index_export(lshg_index* idx, int what, void* dst, size_t* bytes) {
       case 2: src = I.keys.ptr; nb = I.keys.bytes(); break;
       case 3: src = I.offsets.ptr; nb = I.offsets.bytes(); break;
       case 4: src = I.buckets.ptr; nb = I.buckets.bytes(); break;
+      case 5: src = I.qstats.ptr; nb = I.qstats.bytes(); break;
       default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "unknown export item");
     }
     *bytes = nb;

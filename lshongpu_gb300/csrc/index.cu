@@ -241,7 +241,7 @@ Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
   x.release(); xnorm.release(); xt.release(); xs.release(); xsf.release(); xsft.release(); sk_planes.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
-  xbf.release(); xbf_scale.release(); qerr.release();
+  xbf.release(); xbf_scale.release(); qerr.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();
@@ -274,6 +274,8 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
   LSHG_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
   I.qerr.alloc(1, s);
   LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
+  I.qstats.alloc(2, s);
+  LSHG_CUDA(cudaMemsetAsync(I.qstats.ptr, 0, I.qstats.bytes(), s));
   EventTimer tm(s);
   double prep = 0, build = 0;
   float* X = I.x.ptr;
@@ -492,6 +494,8 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     DevBuf<uint32_t> bm((size_t)a.grid * ((I.n + 31) / 32), s);
     LSHG_CUDA(cudaMemsetAsync(bm.ptr, 0, bm.bytes(), s));
     a.bitmaps = bm.ptr;
+    a.vec4 = (I.d % 4 == 0 && (reinterpret_cast<uintptr_t>(I.x.ptr) & 15) == 0) ? 1 : 0;
+    a.stats = I.qstats.ptr;
     launch_lsh_query(a, out, s);
     return;
   }

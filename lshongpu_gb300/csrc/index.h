@@ -77,6 +77,8 @@ struct Index {
   // device error flag of the query path (weighted-MinHash draw limit); read by callers
   // after the query has completed, so the query itself never synchronises
   DevBuf<int> qerr;
+  // query counters (LSH: bucket entries walked, distinct candidates scored), cumulative
+  DevBuf<unsigned long long> qstats;
 
   ~Index();
 };

@@ -120,8 +120,10 @@ struct LshQueryArgs {
   int sdim;
   int C;  // candidate count kept before re-rank (sketched) or pow2 >= k (exact)
   int k;
-  uint32_t* bitmaps;  // per-CTA dedupe bitmaps [grid][ceil(n/32)]
+  uint32_t* bitmaps;  // per-CTA dedupe bitmaps [grid][ceil(n/32)], zero on entry and exit
   int grid;
+  int vec4;                   // rows are 16-byte aligned float4 runs (d % 4 == 0)
+  unsigned long long* stats;  // optional: += bucket entries walked, distinct candidates
 };
 void launch_lsh_query(const LshQueryArgs& a, struct ::lshg_point_s* out, cudaStream_t s);
 

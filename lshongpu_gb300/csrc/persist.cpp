@@ -205,6 +205,8 @@ std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
   fclose(f);
   I.qerr.alloc(1, s);
   LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
+  I.qstats.alloc(2, s);
+  LSHG_CUDA(cudaMemsetAsync(I.qstats.ptr, 0, I.qstats.bytes(), s));
   LSHG_CUDA(cudaStreamSynchronize(s));
   return idx;
 }
