@@ -25,9 +25,9 @@ prints its own line with its own metric; the headline is the default):
 
 `value` is whole-job queries/sec with queries and results resident in HBM; `e2e` is the
 same metric through the C ABI with host (pinned) buffers, every batch's upload and
-download inside the timed region (lshg_index_query_async over two streams, so copies
-overlap the other stream's scan; `e2e.blocking_value` is the one-batch-at-a-time
-lshg_index_query).  `--impl reference` times the reference's CPU brute force (a port of
+download inside the timed region, measured two ways -- lshg_index_query_async over two
+streams (copies overlap the other stream's scan) and the one-batch-at-a-time
+lshg_index_query -- and reported as the better of the two (`e2e.api` names it).  `--impl reference` times the reference's CPU brute force (a port of
 GoldStandard/goldstandard.cpp -- the reference binary is x86-only here) on the host
 cores over a bounded query sample.
 """
@@ -311,17 +311,21 @@ def main():
     ap.add_argument("--path", default=None, choices=["tc", "exact", "simhash", "cplsh", "wmh", "wmh1"])
     ap.add_argument("--config", default=None, choices=sorted(CONFIGS), help="measurement configuration")
     ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
-    ap.add_argument("--n", type=int, default=N_BASE, help="base size (profiling cases only)")
-    ap.add_argument("--nq", type=int, default=N_QUERY, help="queries per step (profiling cases only)")
+    ap.add_argument("--n", type=int, default=None, help="base size (profiling cases only)")
+    ap.add_argument("--nq", type=int, default=None, help="queries per step (profiling cases only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    globals().update(N_BASE=args.n, N_QUERY=args.nq)
     if args.config:
         over = dict(CONFIGS[args.config])
         path = over.pop("path")
         args.path = args.path or path
         globals().update(over)
         globals()["METRIC"] = f"queries/sec, configuration {args.config}"
+    # explicit sizes (small profiling cases) take precedence over a configuration's
+    if args.n is not None:
+        globals()["N_BASE"] = args.n
+    if args.nq is not None:
+        globals()["N_QUERY"] = args.nq
     args.path = args.path or "tc"
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -420,7 +424,7 @@ def main():
     e2e_wait()
     barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    e2e_value = world * N_QUERY / (e2e_ms / 1e3)
+    pipelined_value = world * N_QUERY / (e2e_ms / 1e3)
     # the same with the reference-shaped blocking call (one batch at a time)
     for _ in range(2):
         L.api.check(lib.lshg_index_query(idx.handle, qh.data_ptr(), N_QUERY, K, ohs[0].data_ptr(), 0, sh))
@@ -430,6 +434,11 @@ def main():
         L.api.check(lib.lshg_index_query(idx.handle, qh.data_ptr(), N_QUERY, K, ohs[0].data_ptr(), 0, sh))
     barrier()
     blocking_value = world * N_QUERY / ((time.perf_counter() - t0) / args.steps)
+    # reported: the better of the two ways a caller can drive the ABI (two concurrent LSH
+    # batches contend for L2 -- their dedupe bitmaps -- and lose to one at a time)
+    e2e_value = max(pipelined_value, blocking_value)
+    e2e_api = ("lshg_index_query_async, host buffers, 2 streams" if pipelined_value >= blocking_value
+               else "lshg_index_query, host buffers, one batch at a time")
 
     hbm, bf16, bf16s, peak_kind = peaks()
     lsh_counts = None
@@ -456,6 +465,9 @@ def main():
                 "frac": (achieved / peak) if (achieved and peak) else None, "peak_source": peak_kind,
                 "traffic": traffic, "traffic_unit": "bytes per launch" if traffic else None, "kernel_ms_per_launch": (kms / cnt) if cnt else None,
                 "kernel_share": (kms / sum(v[1] for v in prof.values())) if prof else None}
+    if lsh_counts:
+        roofline["lsh_entries_per_query"] = lsh_counts[0] / N_QUERY
+        roofline["lsh_distinct_per_query"] = lsh_counts[1] / N_QUERY
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -522,8 +534,8 @@ def main():
                    "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
         "roofline": roofline,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERY * (DIM + PAD_DIM) * 4,
-                "d2h_bytes_per_step": N_QUERY * K * 8, "api": "lshg_index_query_async, host buffers, 2 streams",
-                "blocking_value": blocking_value},
+                "d2h_bytes_per_step": N_QUERY * K * 8, "api": e2e_api,
+                "pipelined_value": pipelined_value, "blocking_value": blocking_value},
         "gpu_launches": launches,
         "index_build_s": build_s,
         "clocks": clk.summary(),

@@ -28,6 +28,7 @@ void launch_pack_bytes(const uint8_t* in, int64_t n, int sbytes, uint32_t* out, 
 size_t wmh_state_bytes();
 size_t lsh_query_smem(const LshQueryArgs& a);
 int lsh_query_grid(int nq);
+void lsh_query_plan(LshQueryArgs& a, int max_grid);
 void launch_tc_scan(Index& idx, const float* q, int nq, int k, lshg_point* out, cudaStream_t s);
 void tc_prepare(Index& idx, cudaStream_t s);
 
@@ -444,6 +445,8 @@ void query_error(Index& I, cudaStream_t s) {
   if (e) {
     LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
     if (e == 2) throw Error(LSHG_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out (kernel aborted)");
+    if (e == 3)
+      throw Error(LSHG_ERR_TIMEOUT, "LSH query: a row-copy wait timed out (the rows were re-read directly)");
     throw Error(LSHG_ERR_SAMPLER_LIMIT, "weighted MinHash sampler exceeded its draw limit (zero or NaN query?)");
   }
 }
@@ -489,13 +492,14 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     a.sdim = I.sdim;
     a.C = a.sketched ? std::max(I.C, kp) : kp;
     a.k = k;
-    a.grid = std::min(I.lsh_grid, lsh_query_grid(nq));
+    a.vec4 = (I.d % 4 == 0 && (reinterpret_cast<uintptr_t>(I.x.ptr) & 15) == 0) ? 1 : 0;
+    lsh_query_plan(a, I.lsh_grid);  // staging choice and grid (resident CTAs)
     // per-call dedupe bitmaps: concurrent queries on one index never share them
     DevBuf<uint32_t> bm((size_t)a.grid * ((I.n + 31) / 32), s);
     LSHG_CUDA(cudaMemsetAsync(bm.ptr, 0, bm.bytes(), s));
     a.bitmaps = bm.ptr;
-    a.vec4 = (I.d % 4 == 0 && (reinterpret_cast<uintptr_t>(I.x.ptr) & 15) == 0) ? 1 : 0;
     a.stats = I.qstats.ptr;
+    a.err = I.qerr.ptr;
     launch_lsh_query(a, out, s);
     return;
   }

@@ -124,6 +124,8 @@ struct LshQueryArgs {
   int grid;
   int vec4;                   // rows are 16-byte aligned float4 runs (d % 4 == 0)
   unsigned long long* stats;  // optional: += bucket entries walked, distinct candidates
+  int* err;                   // device error flag (3: a row-copy wait timed out)
+  int stage;                  // set by launch_lsh_query: rows staged by bulk copies
 };
 void launch_lsh_query(const LshQueryArgs& a, struct ::lshg_point_s* out, cudaStream_t s);
 

@@ -8,18 +8,19 @@
 //
 // Query (scan, :142-252 + removeDuplicates, :255-280): one CTA per query gathers the
 // ids of its L buckets (bucket t ends at the next key's offset, or at the table's end
-// for the last key, :183-184), drops repeats with a shared-memory id set backed by a
-// per-CTA bitmap (the reference keeps repeats in its queue and removes adjacent equal
-// ids after sorting), scores each distinct candidate exactly or by sketch, keeps the
-// best C by (distance, id), and for sketched scoring re-ranks them exactly
-// (candidateSetScan, :236-238) before writing the first k.  Fewer than k distinct
-// candidates leave (-1, INT_MAX) entries.
+// for the last key, :183-184), drops repeats with a per-CTA bitmap (the reference keeps
+// repeats in its queue and removes adjacent equal ids after sorting), scores each
+// distinct candidate exactly or by sketch, keeps the best C by (distance, id), and for
+// sketched scoring re-ranks them exactly (candidateSetScan, :236-238) before writing the
+// first k.  Fewer than k distinct candidates leave (-1, INT_MAX) entries.  Exact scoring
+// stages candidate rows in shared memory with bulk copies (see staged_key).
 #include "common.cuh"
 #include "distance.cuh"
 #include "kernels.h"
 #include "launch_count.h"
 #include "profile.h"
 #include "select.cuh"
+#include "tc_ptx.cuh"
 
 namespace lshg {
 
@@ -28,13 +29,15 @@ namespace {
 constexpr int kQThreads = 256;
 constexpr int kQBuf = 2 * kQThreads;
 constexpr int kMaxTables = 256;
-constexpr int kHashBits = 13;                 // shared dedupe set: 8192 ids (32 KB)
-constexpr int kHashSlots = 1 << kHashBits;
-constexpr int kProbe = 32;                    // linear-probe limit before the global bitmap
 constexpr int kUnroll = 4;                    // bucket entries a thread loads per round
 constexpr int kRound = kUnroll * kQThreads;   // entries walked per round
 constexpr int kScoreAt = 1024;                // score the distinct list once it holds this many
 constexpr int kListCap = kScoreAt + kRound;   // a round adds at most kRound ids
+constexpr int kRowBatch = 8;                  // float4 row loads in flight per thread (direct path)
+constexpr int kStageRows = 16;                // rows a warp stages per bulk-copy batch
+constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268 at 16 rows x 8 warps)
+constexpr int kQueryCtasPerSm = 2;            // resident query CTAs an SM (register budget; d = 128
+                                              // staging, 66 KB a CTA, allows two)
 
 __global__ void lsh_hist_kernel(const uint16_t* __restrict__ keys, int64_t n, int tables, int S, int* counts) {
   int64_t total = n * tables;
@@ -108,40 +111,37 @@ __device__ __forceinline__ float sketch_distance(const LshQueryArgs& a, int id, 
   return __fsub_rn(1.0f, __fdiv_rn((float)(32 * a.words - acc), (float)(32 * a.words)));
 }
 
-// Dedupe of one query's bucket entries: a shared-memory open-addressing set of ids
-// (linear probing, at most kProbe slots, filled monotonically within the query), and the
-// CTA's global bitmap for ids whose probe run is full.  An id found in its probe run is
-// never sent to the bitmap, and an id whose run is full can no longer enter the set, so
-// every distinct id is reported new exactly once.
-__device__ __forceinline__ bool dedupe_new(int* hash, uint32_t* bitmap, int id, int* bm_used) {
-  const uint32_t h = ((uint32_t)id * 0x9E3779B1u) >> (32 - kHashBits);
-  for (int p = 0; p < kProbe; ++p) {
-    int* slot = hash + ((h + p) & (kHashSlots - 1));
-    const int v = *reinterpret_cast<volatile int*>(slot);
-    if (v == id) return false;
-    if (v == -1) {
-      const int old = atomicCAS(slot, -1, id);
-      if (old == -1) return true;
-      if (old == id) return false;
-    }
-  }
-  *bm_used = 1;
+// Dedupe of one query's bucket entries on the CTA's bitmap (one bit a base point): the
+// thread whose atomicOr sets an id's bit reports it new, so every distinct id is reported
+// exactly once.  (A shared-memory id set in front of the bitmap measured slower once
+// rows were staged: its 32 KB cost more resident CTAs than it saved in L2 atomics.)
+__device__ __forceinline__ bool dedupe_new(uint32_t* bitmap, int id) {
   const uint32_t bit = 1u << (id & 31);
   return !(atomicOr(&bitmap[id >> 5], bit) & bit);
 }
 
+// Non-coherent 16-byte load, issued where written.
+__device__ __forceinline__ float4 ldg_nc_f4(const float4* p) {
+  float4 v;
+  asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+  return v;
+}
+
 // Exact distance of a 16-byte-aligned row held as d4 float4s: the same operations in the
-// same order as exact_distance, with the row fetched eight float4s at a time.
-template <int DIST>
+// same order as exact_distance, with the row fetched kRowBatch float4s at a time (all
+// loads of a batch issued before its first use).
+// kShared: the row was staged in shared memory.
+template <int DIST, bool kShared = false>
 __device__ __forceinline__ float exact_distance_v4(const float4* __restrict__ xr, const float4* qr, int d4, float qn,
                                                    float xn) {
   float acc = 0.0f, mx = 0.0f;
-  for (int j0 = 0; j0 < d4; j0 += 8) {
-    float4 xv[8];
+  for (int j0 = 0; j0 < d4; j0 += kRowBatch) {
+    float4 xv[kRowBatch];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) xv[u] = j0 + u < d4 ? __ldg(xr + j0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < kRowBatch; ++u)
+      xv[u] = j0 + u < d4 ? (kShared ? xr[j0 + u] : ldg_nc_f4(xr + j0 + u)) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < kRowBatch; ++u) {
       if (j0 + u >= d4) break;
       const float4 qv = qr[j0 + u];
       const float xs[4] = {xv[u].x, xv[u].y, xv[u].z, xv[u].w};
@@ -165,6 +165,59 @@ __device__ __forceinline__ float exact_distance_v4(const float4* __restrict__ xr
   return DIST == DIST_EUCLID ? __fsqrt_rn(acc) : acc;
 }
 
+// Bounded wait on a staging barrier; on timeout raises error 3 (when err is given).
+__device__ __forceinline__ bool stage_wait(uint32_t bar, uint32_t parity, int* err) {
+  if (tc::mbar_try(bar, parity)) return true;
+  const uint64_t t0 = tc::global_ns();
+  while (!tc::mbar_try_sleep(bar, parity, 20000u)) {
+    if (tc::global_ns() - t0 > tc::kWaitNs) {
+      if (err) atomicExch(err, 3);
+      return false;
+    }
+  }
+  return true;
+}
+
+// Key of lane's candidate `id` (-1: none), warp-collective.  Rows are fetched by bulk
+// copies into the warp's staging slots, kStageRows lanes at a time (a 16-byte lane load
+// per row element would cap the gather near 2 TB/s: 32 scattered lines an instruction),
+// then each lane runs its row's chain from shared memory in the same order as
+// exact_distance.  If a copy wait times out, the warp stops staging (ok = false) and
+// reads rows directly from then on; `pending` keeps the parity left incomplete.
+template <int DIST>
+__device__ __forceinline__ uint64_t staged_key(const LshQueryArgs& a, int id, const float* qr, float qn,
+                                               unsigned char* stage, uint32_t bar, uint32_t& phase, bool& ok,
+                                               uint32_t& pending) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t rowb = (uint32_t)a.d * 4u, slot = rowb + 16u;
+  const float xn = (DIST == DIST_ANGULAR && id >= 0) ? a.xnorm[id] : 1.0f;
+  float dist = 0.0f;
+#pragma unroll 1
+  for (int b = 0; b < 32 / kStageRows; ++b) {
+    const bool mine = id >= 0 && (lane / kStageRows) == b;
+    const unsigned m = __ballot_sync(0xffffffffu, mine);
+    if (!m) continue;
+    unsigned char* dst = stage + (uint32_t)(lane % kStageRows) * slot;
+    if (ok) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier slot reads first
+      if (lane == 0) tc::mbar_expect_tx(bar, (uint32_t)__popc(m) * rowb);
+      __syncwarp();
+      if (mine) tc::bulk_load(tc::smem_u32(dst), a.x + (int64_t)id * a.d, rowb, bar);
+      ok = __all_sync(0xffffffffu, stage_wait(bar, phase, a.err));
+      if (!ok) pending = phase;
+      phase ^= 1u;
+    }
+    if (mine) {
+      dist = ok ? exact_distance_v4<DIST, true>(reinterpret_cast<const float4*>(dst),
+                                                reinterpret_cast<const float4*>(qr), a.d >> 2, qn, xn)
+                : exact_distance_v4<DIST, false>(reinterpret_cast<const float4*>(a.x + (int64_t)id * a.d),
+                                                 reinterpret_cast<const float4*>(qr), a.d >> 2, qn, xn);
+    }
+    __syncwarp();
+  }
+  return id >= 0 ? make_key(dist, id) : kEmptyKey;
+}
+
 // Table of flat bucket-entry index idx: the t with pref[t] <= idx < pref[t+1].
 __device__ __forceinline__ int entry_table(const int* pref, int tables, int idx) {
   int lo = 0, hi = tables;
@@ -181,24 +234,36 @@ __device__ __forceinline__ int entry_table(const int* pref, int tables, int idx)
 // they are scored, one thread per candidate, and offered to the top-C queue.  Scoring
 // order does not matter: keys (distance, id) are unique, so the kept set is the same.
 template <int DIST>
-__global__ void __launch_bounds__(kQThreads, 4) lsh_query_kernel(LshQueryArgs a, lshg_point* __restrict__ out) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t* kept = reinterpret_cast<uint64_t*>(smem);
+__global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(LshQueryArgs a, lshg_point* __restrict__ out) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int NW = kQThreads / 32;
+  const uint32_t stage_slot = (uint32_t)a.d * 4u + 16u;
+  const uint32_t stage_bytes = a.stage ? (uint32_t)(NW * kStageRows) * stage_slot : 0u;
+  uint64_t* kept = reinterpret_cast<uint64_t*>(smem + stage_bytes);
   uint64_t* buf = kept + a.C;
   uint64_t* rk = buf + kQBuf;  // re-rank keys [C]
-  int* hash = reinterpret_cast<int*>(rk + a.C);
-  int* list = hash + kHashSlots;
+  int* list = reinterpret_cast<int*>(rk + a.C);
   float* qr = reinterpret_cast<float*>(list + kListCap);
   const int dpad = (a.d + 3) & ~3;
   float* qsf = qr + dpad;
   uint32_t* qsk = reinterpret_cast<uint32_t*>(qsf + (a.sketch_kind == 6 ? a.sdim : 0));
   __shared__ int bstart[kMaxTables], pref[kMaxTables + 1];
-  __shared__ int cnt_s, bm_used_s;
+  __shared__ int cnt_s;
   __shared__ int rcnt[3];  // ids appended per round, cycled: round r uses rcnt[r % 3]
   __shared__ uint64_t thr_s;
   TopCShared S{kept, buf, &cnt_s, &thr_s, a.C, kQBuf};
+  __shared__ __align__(8) uint64_t stage_bar[NW];
   uint32_t* bitmap = a.bitmaps + (int64_t)blockIdx.x * ((a.n + 31) / 32);
   const int tid = threadIdx.x;
+  unsigned char* stage_w = smem + (uint32_t)((tid >> 5) * kStageRows) * stage_slot;
+  const uint32_t bar_w = tc::smem_u32(&stage_bar[tid >> 5]);
+  uint32_t sphase = 0, spending = 0;
+  bool sok = true;  // warp-uniform
+  if (a.stage) {
+    if (tid < NW) tc::mbar_init(tc::smem_u32(&stage_bar[tid]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
 
   for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
     for (int j = tid; j < dpad; j += kQThreads) qr[j] = j < a.d ? a.q[(int64_t)qi * a.d + j] : 0.0f;
@@ -219,12 +284,8 @@ __global__ void __launch_bounds__(kQThreads, 4) lsh_query_kernel(LshQueryArgs a,
       bstart[t] = st;
       pref[t + 1] = en - st;
     }
-    for (int i = tid; i < kHashSlots; i += kQThreads) hash[i] = -1;
     topc_init(S, 1);
-    if (tid == 0) {
-      rcnt[0] = rcnt[1] = rcnt[2] = 0;
-      bm_used_s = 0;
-    }
+    if (tid == 0) rcnt[0] = rcnt[1] = rcnt[2] = 0;
     __syncthreads();
     if (tid == 0) {
       pref[0] = 0;
@@ -252,7 +313,7 @@ __global__ void __launch_bounds__(kQThreads, 4) lsh_query_kernel(LshQueryArgs a,
       }
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
-        if (ids[u] >= 0 && dedupe_new(hash, bitmap, ids[u], &bm_used_s))
+        if (ids[u] >= 0 && dedupe_new(bitmap, ids[u]))
           list[lbase + atomicAdd(&rcnt[r % 3], 1)] = ids[u];
       }
       __syncthreads();
@@ -263,7 +324,11 @@ __global__ void __launch_bounds__(kQThreads, 4) lsh_query_kernel(LshQueryArgs a,
       }
       for (int i0 = 0; i0 < nl; i0 += kQThreads) {
         const int i = i0 + tid;
-        if (i < nl) {
+        if (a.stage) {  // uniform: every lane takes part in the warp's copies
+          const uint64_t key = staged_key<DIST>(a, i < nl ? list[i] : -1, qr, qn, stage_w, bar_w, sphase, sok,
+                                                spending);
+          if (i < nl) topc_push(S, 0, key, thr);
+        } else if (i < nl) {
           const int id = list[i];
           float dist;
           if (a.sketched) {
@@ -276,23 +341,23 @@ __global__ void __launch_bounds__(kQThreads, 4) lsh_query_kernel(LshQueryArgs a,
           }
           topc_push(S, 0, make_key(dist, id), thr);
         }
-        topc_flush(S, 1, kQBuf - kQThreads);
+        // until the kept list is full every key is pushed: fold as soon as it can be
+        // filled, so the first fold sorts at most one sub-round's keys
+        topc_flush<true>(S, 1, thr == kEmptyKey ? a.C - 1 : kQBuf - kQThreads);
         thr = thr_s;
       }
       distinct += nl;
       lbase = 0;  // the list is reused: topc_flush's last barrier follows every read of it
     }
-    topc_flush(S, 1, 0);
+    topc_flush<true>(S, 1, 0);
     if (a.stats && tid == 0) {
       atomicAdd(a.stats, (unsigned long long)total);
       atomicAdd(a.stats + 1, (unsigned long long)distinct);
     }
-    if (bm_used_s) {  // clear the bitmap words this query set (rare: a probe run was full)
-      for (int idx = tid; idx < total; idx += kQThreads) {
-        const int t = entry_table(pref, a.tables, idx);
-        const int id = a.buckets[bstart[t] + (idx - pref[t])];
-        bitmap[id >> 5] = 0u;
-      }
+    for (int idx = tid; idx < total; idx += kQThreads) {  // clear the bitmap words this query set
+      const int t = entry_table(pref, a.tables, idx);
+      const int id = a.buckets[bstart[t] + (idx - pref[t])];
+      bitmap[id >> 5] = 0u;
     }
     const uint64_t* fin = kept;
     if (a.sketched) {
@@ -319,6 +384,7 @@ __global__ void __launch_bounds__(kQThreads, 4) lsh_query_kernel(LshQueryArgs a,
     }
     __syncthreads();
   }
+  if (a.stage && !sok) stage_wait(bar_w, spending, nullptr);  // a timed-out copy may still land
 }
 
 }  // namespace
@@ -343,9 +409,33 @@ void launch_lsh_build(const uint16_t* keys, int64_t n, int tables, int tableSize
   LSHG_CHECK_LAUNCH();
 }
 
+static size_t lsh_stage_bytes(int d) { return (size_t)(kQThreads / 32) * kStageRows * ((size_t)d * 4 + 16); }
+
 size_t lsh_query_smem(const LshQueryArgs& a) {
-  return (size_t)(2 * a.C + kQBuf) * 8 + (size_t)(kHashSlots + kListCap) * 4 + (size_t)((a.d + 3) & ~3) * 4 +
-         (size_t)(a.sketch_kind == 6 ? a.sdim : 0) * 4 + (size_t)a.wp * 4 + 16;
+  return (a.stage ? lsh_stage_bytes(a.d) : 0) + (size_t)(2 * a.C + kQBuf) * 8 + (size_t)kListCap * 4 +
+         (size_t)((a.d + 3) & ~3) * 4 + (size_t)(a.sketch_kind == 6 ? a.sdim : 0) * 4 + (size_t)a.wp * 4 + 16;
+}
+
+template <int DV>
+static int lsh_ctas_per_sm(size_t smem) {
+  LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per = 0;
+  LSHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lsh_query_kernel<DV>, kQThreads, smem));
+  return per;
+}
+
+void lsh_query_plan(LshQueryArgs& a, int max_grid) {
+  a.stage = (a.vec4 && !a.sketched && lsh_stage_bytes(a.d) <= (size_t)kStageMaxBytes) ? 1 : 0;
+  const size_t smem = lsh_query_smem(a);
+  int per = 1;
+  if (smem <= 200 * 1024) {
+    switch (a.dist) {
+      case DIST_ANGULAR: per = lsh_ctas_per_sm<DIST_ANGULAR>(smem); break;
+      case DIST_JACCARD: per = lsh_ctas_per_sm<DIST_JACCARD>(smem); break;
+      default: per = lsh_ctas_per_sm<DIST_EUCLID>(smem); break;
+    }
+  }
+  a.grid = std::max(1, std::min(std::min(max_grid, a.nq), num_sms() * std::max(1, per)));
 }
 
 void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
@@ -373,6 +463,6 @@ void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
   LSHG_CHECK_LAUNCH();
 }
 
-int lsh_query_grid(int nq) { return std::max(1, std::min(nq, num_sms() * 4)); }
+int lsh_query_grid(int nq) { return std::max(1, std::min(nq, num_sms() * kQueryCtasPerSm)); }
 
 }  // namespace lshg

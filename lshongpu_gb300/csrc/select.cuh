@@ -105,6 +105,50 @@ __device__ __forceinline__ void warp_fold_buffer(uint64_t* kept, int C, uint64_t
   warp_bitonic_merge(kept, C);
 }
 
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint64_t (&x)[E], int lane, bool merge_only);
+
+template <int E>
+__device__ __forceinline__ void warp_sort_buffer_regs(uint64_t* buf, int cnt, int nb) {
+  const int lane = threadIdx.x & 31;
+  uint64_t x[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int i = e * 32 + lane;
+    x[e] = i < cnt ? buf[i] : kEmptyKey;
+  }
+  warp_bitonic<E>(x, lane, false);
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < E; ++e)
+    if (e * 32 + lane < nb) buf[e * 32 + lane] = x[e];
+  __syncwarp();
+}
+
+// warp_fold_buffer with buffers of up to 256 keys sorted in registers (a shuffle
+// network: no chain of dependent shared-memory round trips); larger ones as before.
+// Same result, same room requirement.
+static __device__ __noinline__ void warp_fold_buffer_regs(uint64_t* kept, int C, uint64_t* buf, int cnt) {
+  const int lane = threadIdx.x & 31;
+  if (cnt <= 0) return;
+  const int nb = next_pow2_dev(cnt < 2 ? 2 : cnt);
+  if (nb > 256) {
+    warp_fold_buffer(kept, C, buf, cnt);
+    return;
+  }
+  if (nb <= 32) warp_sort_buffer_regs<1>(buf, cnt, nb);
+  else if (nb <= 64) warp_sort_buffer_regs<2>(buf, cnt, nb);
+  else if (nb <= 128) warp_sort_buffer_regs<4>(buf, cnt, nb);
+  else warp_sort_buffer_regs<8>(buf, cnt, nb);
+  for (int i = lane; i < C; i += 32) {
+    const int j = C - 1 - i;
+    const uint64_t b = (j < nb) ? buf[j] : kEmptyKey;
+    if (b < kept[i]) kept[i] = b;
+  }
+  __syncwarp();
+  warp_bitonic_merge(kept, C);
+}
+
 // Per-query selection state in shared memory, laid out by the kernel:
 //   kept[q*C .. q*C+C)   sorted ascending
 //   buf [q*B .. q*B+B)   append buffer
@@ -137,6 +181,8 @@ __device__ __forceinline__ void topc_push(TopCShared s, int q, uint64_t key, uin
 // Merge the buffers of every query whose fill exceeds `limit` (or all non-empty buffers
 // when limit < 0).  Block-wide: all threads call it; warps take queries round-robin.
 // Returns after a __syncthreads so new thresholds are visible.
+// kRegSort: fold with warp_fold_buffer_regs.
+template <bool kRegSort = false>
 __device__ __forceinline__ void topc_flush(TopCShared s, int nq, int limit) {
   __syncthreads();
   const int warp = threadIdx.x >> 5;
@@ -144,7 +190,8 @@ __device__ __forceinline__ void topc_flush(TopCShared s, int nq, int limit) {
   for (int q = warp; q < nq; q += nwarps) {
     int c = s.cnt[q];
     if (c > limit && c > 0) {
-      warp_fold_buffer(s.kept + (size_t)q * s.C, s.C, s.buf + (size_t)q * s.B, c);
+      if (kRegSort) warp_fold_buffer_regs(s.kept + (size_t)q * s.C, s.C, s.buf + (size_t)q * s.B, c);
+      else warp_fold_buffer(s.kept + (size_t)q * s.C, s.C, s.buf + (size_t)q * s.B, c);
       if ((threadIdx.x & 31) == 0) {
         s.cnt[q] = 0;
         s.thr[q] = s.kept[(size_t)q * s.C + s.C - 1];

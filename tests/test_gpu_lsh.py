@@ -47,6 +47,50 @@ def test_crosspoly_keys_buckets_query(engine, orc, hashes, bits):
     assert np.array_equal(res["distance"], ds)
 
 
+def walked_and_distinct(qkeys, off, bk, tables, S, n):
+    """Bucket entries each query walks and its distinct candidates, from the oracle's tables."""
+    ent, dis = [], []
+    for row in qkeys:
+        parts = []
+        for t in range(tables):
+            key = int(row[t])
+            st = off[t * S + key]
+            en = off[t * S + key + 1] if key + 1 < S else t * n + n
+            parts.append(bk[st:en])
+        a = np.concatenate(parts)
+        ent.append(a.size)
+        dis.append(np.unique(a).size)
+    return np.array(ent), np.array(dis)
+
+
+@pytest.mark.parametrize("d,P", [(100, 128), (37, 64)])
+def test_crosspoly_many_candidates_and_counters(engine, orc, d, P):
+    """~20k distinct candidates a query (many scoring batches per query) and 640 queries,
+    more than the query kernel's resident CTAs, so CTAs answer further queries after
+    clearing their dedupe bitmaps.  d = 37 takes the direct row path, d = 100 the rows
+    staged by bulk copies.  The kernel's counters must equal the entries walked and the
+    distinct candidates computed from the oracle's tables."""
+    n, nq, L, bits = 40000, 640, 12, 8
+    x = datasets.clustered(n, d, 61, count=2)
+    q = datasets.clustered(nq, d, 62, count=2)
+    S = 1 << bits
+    idx = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=bits,
+                       tables=L, options=engine.make_options(cp_hashes=1))
+    xn, qn = orc.normalize(x), orc.normalize(q)
+    diag = engine.random_plus_minus(P * L * 3)
+    okeys = orc.crosspoly(xn, P, L, 1, 3, diag)
+    oqk = orc.crosspoly(qn, P, L, 1, 3, diag)
+    ooff, obk = orc.lsh_build(okeys, L, S)
+    ent, dis = walked_and_distinct(oqk, ooff, obk, L, S, n)
+    assert dis.min() > 8192  # the case this test is for
+    assert idx.query_counters() == (0, 0)
+    res = idx.query(q, 32)
+    ids, ds = orc.lsh_query(xn, qn, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, 1, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
+    assert idx.query_counters() == (int(ent.sum()), int(dis.sum()))
+
+
 def test_simhash_keys_sketched_query(engine, orc):
     n, nq, L, bits, W = 3000, 12, 6, 10, 8
     x, q = data(n, nq, seed=31)
