@@ -445,8 +445,7 @@ void query_error(Index& I, cudaStream_t s) {
   if (e) {
     LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
     if (e == 2) throw Error(LSHG_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out (kernel aborted)");
-    if (e == 3)
-      throw Error(LSHG_ERR_TIMEOUT, "LSH query: a row-copy wait timed out (the rows were re-read directly)");
+    if (e == 3) throw Error(LSHG_ERR_TIMEOUT, "a row-copy wait timed out (the rows were re-read directly)");
     throw Error(LSHG_ERR_SAMPLER_LIMIT, "weighted MinHash sampler exceeded its draw limit (zero or NaN query?)");
   }
 }
@@ -542,7 +541,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     launch_merge_splits(part.ptr, nq, splits, C, merged.ptr, s);
     cand = merged.ptr;
   }
-  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s);
+  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.qerr.ptr);
 }
 
 }  // namespace lshg

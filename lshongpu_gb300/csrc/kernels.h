@@ -84,7 +84,7 @@ void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t
 // Exact re-rank of candidate keys (candidateSetScanner.cuh:10-32) and top-k output.
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d,
                    const float* xnorm, const float* q, const float* qnorm, int dist, int k,
-                   struct ::lshg_point_s* out, cudaStream_t s);
+                   struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr);
 // Keys to result points (ID, distance); empty keys become (-1, INT_MAX).
 void launch_keys_to_points(const uint64_t* keys, int nq, int C, int k, struct ::lshg_point_s* out,
                            cudaStream_t s);

@@ -33,7 +33,6 @@ constexpr int kUnroll = 4;                    // bucket entries a thread loads p
 constexpr int kRound = kUnroll * kQThreads;   // entries walked per round
 constexpr int kScoreAt = 1024;                // score the distinct list once it holds this many
 constexpr int kListCap = kScoreAt + kRound;   // a round adds at most kRound ids
-constexpr int kRowBatch = 8;                  // float4 row loads in flight per thread (direct path)
 constexpr int kStageRows = 16;                // rows a warp stages per bulk-copy batch
 constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268 at 16 rows x 8 warps)
 constexpr int kQueryCtasPerSm = 2;            // resident query CTAs an SM (register budget; d = 128
@@ -120,50 +119,6 @@ __device__ __forceinline__ bool dedupe_new(uint32_t* bitmap, int id) {
   return !(atomicOr(&bitmap[id >> 5], bit) & bit);
 }
 
-// Non-coherent 16-byte load, issued where written.
-__device__ __forceinline__ float4 ldg_nc_f4(const float4* p) {
-  float4 v;
-  asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
-  return v;
-}
-
-// Exact distance of a 16-byte-aligned row held as d4 float4s: the same operations in the
-// same order as exact_distance, with the row fetched kRowBatch float4s at a time (all
-// loads of a batch issued before its first use).
-// kShared: the row was staged in shared memory.
-template <int DIST, bool kShared = false>
-__device__ __forceinline__ float exact_distance_v4(const float4* __restrict__ xr, const float4* qr, int d4, float qn,
-                                                   float xn) {
-  float acc = 0.0f, mx = 0.0f;
-  for (int j0 = 0; j0 < d4; j0 += kRowBatch) {
-    float4 xv[kRowBatch];
-#pragma unroll
-    for (int u = 0; u < kRowBatch; ++u)
-      xv[u] = j0 + u < d4 ? (kShared ? xr[j0 + u] : ldg_nc_f4(xr + j0 + u)) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int u = 0; u < kRowBatch; ++u) {
-      if (j0 + u >= d4) break;
-      const float4 qv = qr[j0 + u];
-      const float xs[4] = {xv[u].x, xv[u].y, xv[u].z, xv[u].w};
-      const float qs[4] = {qv.x, qv.y, qv.z, qv.w};
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        if (DIST == DIST_ANGULAR) {
-          acc = __fmaf_rn(qs[e], xs[e], acc);
-        } else if (DIST == DIST_JACCARD) {
-          acc = __fadd_rn(acc, fminf(xs[e], qs[e]));
-          mx = __fadd_rn(mx, fmaxf(xs[e], qs[e]));
-        } else {
-          const float df = __fsub_rn(qs[e], xs[e]);
-          acc = __fmaf_rn(df, df, acc);
-        }
-      }
-    }
-  }
-  if (DIST == DIST_ANGULAR) return __fsub_rn(1.0f, __fdiv_rn(acc, __fmul_rn(qn, xn)));
-  if (DIST == DIST_JACCARD) return __fsub_rn(1.0f, __fdiv_rn(acc, mx));
-  return DIST == DIST_EUCLID ? __fsqrt_rn(acc) : acc;
-}
 
 // Bounded wait on a staging barrier; on timeout raises error 3 (when err is given).
 __device__ __forceinline__ bool stage_wait(uint32_t bar, uint32_t parity, int* err) {
@@ -189,7 +144,7 @@ __device__ __forceinline__ uint64_t staged_key(const LshQueryArgs& a, int id, co
                                                unsigned char* stage, uint32_t bar, uint32_t& phase, bool& ok,
                                                uint32_t& pending) {
   const int lane = threadIdx.x & 31;
-  const uint32_t rowb = (uint32_t)a.d * 4u, slot = rowb + 16u;
+  const uint32_t rowb = (uint32_t)a.d * 4u, slot = stage_slot_bytes(a.d);
   const float xn = (DIST == DIST_ANGULAR && id >= 0) ? a.xnorm[id] : 1.0f;
   float dist = 0.0f;
 #pragma unroll 1
@@ -237,7 +192,7 @@ template <int DIST>
 __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(LshQueryArgs a, lshg_point* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int NW = kQThreads / 32;
-  const uint32_t stage_slot = (uint32_t)a.d * 4u + 16u;
+  const uint32_t stage_slot = stage_slot_bytes(a.d);
   const uint32_t stage_bytes = a.stage ? (uint32_t)(NW * kStageRows) * stage_slot : 0u;
   uint64_t* kept = reinterpret_cast<uint64_t*>(smem + stage_bytes);
   uint64_t* buf = kept + a.C;
@@ -409,7 +364,7 @@ void launch_lsh_build(const uint16_t* keys, int64_t n, int tables, int tableSize
   LSHG_CHECK_LAUNCH();
 }
 
-static size_t lsh_stage_bytes(int d) { return (size_t)(kQThreads / 32) * kStageRows * ((size_t)d * 4 + 16); }
+static size_t lsh_stage_bytes(int d) { return (size_t)(kQThreads / 32) * kStageRows * stage_slot_bytes(d); }
 
 size_t lsh_query_smem(const LshQueryArgs& a) {
   return (a.stage ? lsh_stage_bytes(a.d) : 0) + (size_t)(2 * a.C + kQBuf) * 8 + (size_t)kListCap * 4 +

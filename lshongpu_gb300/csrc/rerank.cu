@@ -12,6 +12,7 @@
 #include "select.cuh"
 #include "distance.cuh"
 #include "profile.h"
+#include "tc_ptx.cuh"
 
 namespace lshg {
 
@@ -71,6 +72,90 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
   }
 }
 
+// The same re-rank with the candidate rows staged in shared memory by bulk copies, one
+// row per thread and blockDim rows per chunk (per-thread 4- or 16-byte loads of scattered
+// rows top out near 2 TB/s; bulk copies keep several hundred rows in flight per SM).
+// Needs d % 4 == 0 and 16-byte aligned rows.  A copy wait that times out raises error 3
+// on `err` and the rows are read directly from then on (results are unchanged).
+template <int DIST>
+__global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
+                                     int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
+                                     const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, int* err) {
+  extern __shared__ __align__(128) unsigned char rsm[];
+  const int CH = blockDim.x;
+  const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
+  unsigned char* stage = rsm;
+  uint64_t* keys = reinterpret_cast<uint64_t*>(rsm + (size_t)CH * slot);
+  float* qr = reinterpret_cast<float*>(keys + C);
+  __shared__ __align__(8) uint64_t bar;
+  const int qi = blockIdx.x, tid = threadIdx.x;
+  const uint32_t bar_a = tc::smem_u32(&bar);
+  if (tid == 0) tc::mbar_init(bar_a, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
+  __syncthreads();
+  const float qn = (DIST == DIST_ANGULAR) ? qnorm[qi] : 1.0f;
+  unsigned char* dst = stage + (size_t)tid * slot;
+  uint32_t phase = 0, pending = 0;
+  bool ok = true;  // block-uniform
+  for (int c0 = 0; c0 < C; c0 += CH) {
+    const int i = c0 + tid;
+    int id = -1;
+    if (i < C) {
+      const uint64_t kin = cand[(int64_t)qi * C + i];
+      if (kin != kEmptyKey) {
+        id = key_id(kin);
+        if (id < 0 || id >= n) id = -1;
+      }
+    }
+    const float xn = (DIST == DIST_ANGULAR && id >= 0) ? xnorm[id] : 1.0f;
+    const int nv = __syncthreads_count(id >= 0);
+    if (ok && nv > 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // this thread's earlier slot reads first
+      if (tid == 0) tc::mbar_expect_tx(bar_a, (uint32_t)nv * rowb);
+      __syncthreads();
+      if (id >= 0) tc::bulk_load(tc::smem_u32(dst), x + (int64_t)id * d, rowb, bar_a);
+      bool got = tc::mbar_try(bar_a, phase);
+      if (!got) {
+        const uint64_t t0 = tc::global_ns();
+        while (!(got = tc::mbar_try_sleep(bar_a, phase, 20000u)))
+          if (tc::global_ns() - t0 > tc::kWaitNs) break;
+      }
+      ok = __syncthreads_and(got);
+      if (!ok) {
+        pending = phase;
+        if (tid == 0 && err) atomicExch(err, 3);
+      }
+      phase ^= 1u;
+    }
+    if (i < C) {
+      uint64_t ko = kEmptyKey;
+      if (id >= 0) {
+        const float dist =
+            ok ? exact_distance_v4<DIST, true>(reinterpret_cast<const float4*>(dst), reinterpret_cast<const float4*>(qr),
+                                               d >> 2, qn, xn)
+               : exact_distance<DIST>(x + (int64_t)id * d, qr, d, qn, xn);
+        ko = make_key(dist, id);
+      }
+      keys[i] = ko;
+    }
+  }
+  __syncthreads();
+  block_bitonic_sort(keys, C);
+  for (int i = tid; i < k; i += CH) {
+    const uint64_t kk = i < C ? keys[i] : kEmptyKey;
+    lshg_point pt;
+    if (kk == kEmptyKey) { pt.ID = -1; pt.distance = kEmptyDistance; }
+    else { pt.ID = key_id(kk); pt.distance = key_dist(kk); }
+    out[(int64_t)qi * k + i] = pt;
+  }
+  if (!ok) {  // a timed-out copy may still land: wait for it (bounded) before the block exits
+    const uint64_t t0 = tc::global_ns();
+    while (!tc::mbar_try_sleep(bar_a, pending, 20000u))
+      if (tc::global_ns() - t0 > tc::kWaitNs) break;
+  }
+}
+
 __global__ void keys_to_points_kernel(const uint64_t* __restrict__ keys, int nq, int C, int k,
                                       lshg_point* __restrict__ out) {
   int64_t total = (int64_t)nq * k;
@@ -98,12 +183,34 @@ void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t
 }
 
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d, const float* xnorm,
-                   const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s) {
+                   const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s, int* err) {
   if (nq <= 0) return;
   LSHG_REQUIRE((C & (C - 1)) == 0 && C >= 2, "re-rank: candidate count must be a power of two");
+  ProfScope _ps("rerank", s);
+  // staged: rows of d % 4 == 0 floats, 16-byte aligned, up to 128 a chunk
+  const int CH = std::min(C, 128);
+  const size_t staged_smem = (size_t)CH * stage_slot_bytes(d) + (size_t)C * 8 + (size_t)d * 4 + 16;
+  if (d % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 && staged_smem <= 96 * 1024) {
+#define LSHG_RRS(DV)                                                                                           \
+  do {                                                                                                         \
+    LSHG_CUDA(cudaFuncSetAttribute(rerank_staged_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                   (int)staged_smem));                                                         \
+    rerank_staged_kernel<DV><<<nq, CH, staged_smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, err); \
+  } while (0)
+    switch (dist) {
+      case DIST_ANGULAR: LSHG_RRS(DIST_ANGULAR); break;
+      case DIST_JACCARD: LSHG_RRS(DIST_JACCARD); break;
+      case DIST_EUCLID: LSHG_RRS(DIST_EUCLID); break;
+      case DIST_SQEUCLID: LSHG_RRS(DIST_SQEUCLID); break;
+      default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "re-rank: invalid distance function");
+    }
+#undef LSHG_RRS
+    count_launch();
+    LSHG_CHECK_LAUNCH();
+    return;
+  }
   size_t smem = (size_t)C * 8 + (size_t)d * 4 + 16;
   LSHG_REQUIRE(smem <= 200 * 1024, "re-rank: candidate set too large");
-  ProfScope _ps("rerank", s);
   int threads = C >= 256 ? 256 : 128;
 #define LSHG_RR(DV)                                                                                       \
   do {                                                                                                    \
