@@ -16,7 +16,8 @@ prints its own line with its own metric; the headline is the default):
 
   1       exact angular k-NN, N = 100k, d = 100, Q = 1000, k = 32 (--path exact or tc)
   2       1024-bit SimHash, N = 1.2M, Q = 10k, C = 1024 candidates re-ranked (2-c128: C = 128)
-  3       tensor-core exact scan, N = 1M, d = 128 (100 + 28 zero dims), Q = 16,384
+  3       tensor-core exact scan, N = 1M, d = 128 (100 + 28 zero dims), Q = 16,384 (3-fp8:
+          E4M3 tensor-core scores; --path tc8 runs E4M3 at any size)
   4a      cross-polytope LSH, L = 32 tables, K = 2 hashes a key, 3 rounds, N = 1M, d = 128
           padded, Q = 10k, exact angular distance on candidates (4a-k1: K = 1)
   4b      weighted MinHash, 256 byte samples, N = 500k, d = 100 sparse Gamma(2,1) values
@@ -61,6 +62,7 @@ CONFIGS = {
     "2": dict(path="simhash", CAND=1024),
     "2-c128": dict(path="simhash", CAND=128),
     "3": dict(path="tc", N_BASE=1_000_000, N_QUERY=16_384, PAD_DIM=28),
+    "3-fp8": dict(path="tc8", N_BASE=1_000_000, N_QUERY=16_384, PAD_DIM=28),
     "4a": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=2),
     "4a-k1": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=1),
     "4b": dict(path="wmh", N_BASE=500_000, DATA="sparse"),
@@ -142,6 +144,8 @@ def make_data(seed_offset: int):
 def build_index(L, x, path: str):
     if path == "tc":
         return L.Index(x, implementation=L.IMPL_TC, distanceFunc=1, options=L.make_options(candidates=64))
+    if path == "tc8":
+        return L.Index(x, implementation=L.IMPL_TC_FP8, distanceFunc=1)
     if path == "exact":
         return L.Index(x, implementation=2, distanceFunc=1)
     if path == "simhash":
@@ -170,6 +174,8 @@ def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
     d = DIM
     if path == "tc":
         return "tc_filter", "tensor", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
+    if path == "tc8":
+        return "tc_filter", "tensor8", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
     if path == "exact":
         return "scan_float", "fp32", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
     # sketch scans are integer-bound at these batch sizes: work = sketch words compared
@@ -263,7 +269,8 @@ def workload_text(args) -> str:
     d = f"{DIM}" if not PAD_DIM else f"{DIM + PAD_DIM} ({DIM} + {PAD_DIM} zero dims)"
     data = ("sparse Gamma(2,1) values, 30% nonzero" if DATA == "sparse"
             else "clustered unit vectors (1000 clusters, sigma 0.05)")
-    what = {"tc": "tensor-core exact scan", "exact": "FP32 SIMT exact scan",
+    what = {"tc": "tensor-core exact scan", "tc8": "tensor-core exact scan, E4M3 (FP8) scores",
+            "exact": "FP32 SIMT exact scan",
             "simhash": f"1024-bit SimHash, {CAND} candidates re-ranked",
             "cplsh": f"cross-polytope LSH, L=32, K={CP_HASHES}, 3 rounds, exact angular on candidates",
             "wmh": "weighted MinHash, 256 byte samples, Jaccard scan + generalized-Jaccard re-rank",
@@ -308,7 +315,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--path", default=None, choices=["tc", "exact", "simhash", "cplsh", "wmh", "wmh1"])
+    ap.add_argument("--path", default=None, choices=["tc", "tc8", "exact", "simhash", "cplsh", "wmh", "wmh1"])
     ap.add_argument("--config", default=None, choices=sorted(CONFIGS), help="measurement configuration")
     ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
     ap.add_argument("--n", type=int, default=None, help="base size (profiling cases only)")
@@ -453,6 +460,8 @@ def main():
         peak, peak_kind = FP32_SIMT_NOMINAL_TFLOPS, "nominal (152 SMs x 128 FMA/clk x 2 x 2.07 GHz)"
     elif bound == "tensor":
         peak = bf16
+    elif bound == "tensor8":  # no measured FP8 figure: the dense FP8 rate is twice BF16's
+        peak, peak_kind = 2 * bf16, "2 x measured bf16 (dense FP8 rate = 2 x BF16)"
     elif bound == "popc":
         peak, peak_kind = POPC_NOMINAL_GWORDS, "nominal (152 SMs x 16 popc/clk x 2.07 GHz)"
     else:
@@ -528,7 +537,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {"tc": "bf16", "simhash": "u32", "wmh": "u8", "wmh1": "u32"}.get(args.path, "f32"),
+        "dtype": {"tc": "bf16", "tc8": "e4m3", "simhash": "u32", "wmh": "u8", "wmh1": "u32"}.get(args.path, "f32"),
         "data": "synthetic",
         "config": {"workload": workload_text(args), "global_batch": N_QUERY * world,
                    "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},

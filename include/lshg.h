@@ -23,7 +23,9 @@
  *                            exact scan), 2 = exact linear scan, 3 = SimHash,
  *                            4 = weighted MinHash (byte), 5 = one-bit weighted MinHash,
  *                            6 = Johnson-Lindenstrauss,
- *                            8 = tensor-core exact scan (BF16, no reference counterpart)
+ *                            8 = tensor-core exact scan (BF16, no reference counterpart),
+ *                            9 = the same with E4M3 (FP8) tensor-core scores; both
+ *                                return exact FP32 distances of their candidates
  *   keysImplementation:  3 = SimHash, 4 = WMH byte, 5 = one-bit WMH, 7 = cross-polytope
  *   distanceFunc:        1 = angular, 2 = generalized Jaccard, 3 = Euclidean
  */

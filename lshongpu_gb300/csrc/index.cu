@@ -242,7 +242,7 @@ Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
   x.release(); xnorm.release(); xt.release(); xs.release(); xsf.release(); xsft.release(); sk_planes.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
-  xbf.release(); xbf_scale.release(); qerr.release(); qstats.release();
+  xbf.release(); xbf_scale.release(); xf8.release(); qerr.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();
@@ -281,7 +281,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
   double prep = 0, build = 0;
   float* X = I.x.ptr;
 
-  LSHG_REQUIRE(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8,
+  LSHG_REQUIRE(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8 || impl == 9,
                "Invalid implementation selected");
   LSHG_REQUIRE(p.framework == 0 || p.framework == 1, "framework must be 0 (linear scan) or 1 (LSH)");
 
@@ -289,6 +289,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
     switch (impl) {
       case 2:
       case 8:
+      case 9:
         I.dist = p.distanceFunc;
         LSHG_REQUIRE(I.dist >= 1 && I.dist <= 3, "Invalid operation selected for distance function");
         if (I.dist == DIST_JACCARD) {  // memOptimizedLinearScan.cu:149-163
@@ -311,7 +312,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
   } else {
     I.dist = p.distanceFunc;
     LSHG_REQUIRE(I.dist >= 1 && I.dist <= 3, "Invalid operation selected for distance function");
-    LSHG_REQUIRE(impl != 8, "the tensor-core scan is a linear scan");
+    LSHG_REQUIRE(impl != 8 && impl != 9, "the tensor-core scan is a linear scan");
     LSHG_REQUIRE(p.tables >= 1 && p.tables <= 256, "tables must be in [1, 256]");
     LSHG_REQUIRE(p.bucketKeyBits >= 1 && p.bucketKeyBits <= 24, "bucketKeyBits must be in [1, 24]");
     I.tables = p.tables;
@@ -421,7 +422,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
     I.xt.alloc((size_t)ceil_div(n, 128) * 128 * d, s);
     launch_tile_transpose(X, n, d, I.xt.ptr, s);
   }
-  if (p.framework == 0 && impl == 8) tc_prepare(I, s);
+  if (p.framework == 0 && (impl == 8 || impl == 9)) tc_prepare(I, s);
   if (p.framework == 1) I.lsh_grid = lsh_query_grid(1 << 30);
   check_err_flag(err.ptr, s);
   build += tm.ms();
@@ -502,7 +503,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     launch_lsh_query(a, out, s);
     return;
   }
-  if (impl == 8) {
+  if (impl == 8 || impl == 9) {
     launch_tc_scan(I, q, nq, k, out, s);
     return;
   }

@@ -71,7 +71,8 @@ struct Index {
 
   // tensor-core exact scan (implementation 8)
   DevBuf<uint16_t> xbf;      // bf16 rows padded to dp
-  DevBuf<float> xbf_scale;   // unused for bf16 (kept for an fp8 layout)
+  DevBuf<float> xbf_scale;   // unused (kept for the file layout)
+  DevBuf<uint8_t> xf8;       // E4M3 unit rows x kE4M3Scale, 128 bytes (implementation 9)
   int dp = 0;
 
   // device error flag of the query path (weighted-MinHash draw limit); read by callers

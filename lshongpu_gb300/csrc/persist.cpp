@@ -13,7 +13,7 @@ using namespace lshg;
 
 namespace {
 
-constexpr char kMagic[8] = {'L', 'S', 'H', 'G', 'I', 'D', 'X', '1'};
+constexpr char kMagic[8] = {'L', 'S', 'H', 'G', 'I', 'D', 'X', '2'};
 
 struct Writer {
   FILE* f;
@@ -152,6 +152,7 @@ void buffers_io(IO& io, Index& I, cudaStream_t s) {
   io.dev(I.cp_diag, s);
   io.dev(I.xbf, s);
   io.dev(I.xbf_scale, s);
+  io.dev(I.xf8, s);
   wmh_io(io, I.wmh_sk, s);
   wmh_io(io, I.wmh_keys, s);
 }

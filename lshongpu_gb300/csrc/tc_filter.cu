@@ -47,21 +47,29 @@ namespace {
 
 constexpr int F_THREADS = 640;
 constexpr int TN = FILTER_TN;                   // base points a tile = UMMA N
-constexpr int B_HALF = TN * KHALF * 2;          // 32 KB: one 64-column half of a base tile
-constexpr int B_TILE = 2 * B_HALF;              // 64 KB
-constexpr int F_STAGES = 2;
+constexpr int B_HALF = TN * KHALF * 2;          // 32 KB: one 64-column half of a BF16 base tile
 constexpr int F_NACC = 2;                       // TMEM accumulators of TN columns
 constexpr int F_TMEM_COLS = F_NACC * TN;        // 512 = all of TMEM (one CTA per SM)
 constexpr int F_EPI_WARPS = 16;  // four warpgroups, one 64-column piece each
 
 constexpr int F_SBUF = 8;  // staged survivors a row and warpgroup (flushed with one atomic)
 
-constexpr int F_A_OFF = 0;                                // two query tiles
-constexpr int F_B_OFF = 2 * TILE_BYTES;                   // F_STAGES base tiles
-constexpr int F_S_OFF = F_B_OFF + F_STAGES * B_TILE;      // survivor staging: scores then ids, [4][F_SBUF][BM]
-constexpr int F_BAR_OFF = F_S_OFF + 4 * F_SBUF * BM * 8;
-constexpr int F_SMEM = F_BAR_OFF + 256 + 1024;            // + barriers + 1 KB alignment slack
-static_assert(F_SMEM <= 232448, "shared memory per CTA");
+// Shared-memory layout by operand format.  BF16: a tile row is two 128-byte swizzle rows
+// (64 columns each); E4M3: one (all 128 columns), so tiles are half the size and the
+// base ring has twice the stages.
+template <bool F8>
+struct FLayout {
+  static constexpr int A_BYTES = F8 ? BM * 128 : TILE_BYTES;  // query tile: 16 or 32 KB
+  static constexpr int B_BYTES = F8 ? TN * 128 : 2 * B_HALF;  // base tile: 32 or 64 KB
+  static constexpr int STAGES = F8 ? 4 : 2;
+  static constexpr int A_OFF = 0;                             // two query tiles
+  static constexpr int B_OFF = 2 * A_BYTES;                   // STAGES base tiles
+  static constexpr int S_OFF = B_OFF + STAGES * B_BYTES;      // survivor staging: scores then ids, [4][F_SBUF][BM]
+  static constexpr int BAR_OFF = S_OFF + 4 * F_SBUF * BM * 8;
+  static constexpr int SMEM = BAR_OFF + 256 + 1024;           // + barriers + 1 KB alignment slack
+  static_assert(SMEM <= 232448, "shared memory per CTA");
+  static_assert(8 * (2 * STAGES + 5 + 2 * F_NACC) + 8 <= 256, "barrier area");
+};
 
 struct FilterArgs {
   int nq;
@@ -77,7 +85,7 @@ struct FilterArgs {
   int* cnt;          // survivors per query
   uint64_t* cand;    // [nq][cap] survivor keys
   int cap;
-  int ksteps;    // K=16 MMA steps covering the data dimension
+  int ksteps;    // MMA K steps covering the data dimension (K = 16 BF16 or 32 E4M3 a step)
   int hi_cols;   // columns loaded of the second 64-column half of a base tile
   int* err;
 };
@@ -94,10 +102,15 @@ __device__ __forceinline__ void flush_staged(int* cnt, uint64_t* dst, int cap, c
   }
 }
 
-template <int MODE, int GW>
+// F8: E4M3 operands (kind::f8f6f4); mapBhi is unused.
+template <int MODE, int GW, bool F8>
 __global__ void __launch_bounds__(F_THREADS, 1)
     tc_filter_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                      const __grid_constant__ CUtensorMap mapBhi, const FilterArgs a) {
+  using LY = FLayout<F8>;
+  constexpr int F_STAGES = LY::STAGES;
+  constexpr int F_A_OFF = LY::A_OFF, F_B_OFF = LY::B_OFF, F_S_OFF = LY::S_OFF, F_BAR_OFF = LY::BAR_OFF;
+  constexpr int A_BYTES = LY::A_BYTES, B_TILE = LY::B_BYTES;
   static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column pieces");
   static_assert(GW == 64 || GW == 8, "group width");
   const int U = a.NCH * a.QT;
@@ -153,17 +166,22 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
         const int ab = ua & 1;
         if (!mbar_wait(A_EMPTY(ab), ((ua >> 1) & 1) ^ 1, abort_flag)) break;
-        mbar_expect_tx(A_FULL(ab), TILE_BYTES);
-        tma_load_2d(s0 + F_A_OFF + ab * TILE_BYTES, &mapA, 0, qt * BM, A_FULL(ab));
-        tma_load_2d(s0 + F_A_OFF + ab * TILE_BYTES + HALF_BYTES, &mapA, KHALF, qt * BM, A_FULL(ab));
+        mbar_expect_tx(A_FULL(ab), A_BYTES);
+        tma_load_2d(s0 + F_A_OFF + ab * A_BYTES, &mapA, 0, qt * BM, A_FULL(ab));
+        if (!F8) tma_load_2d(s0 + F_A_OFF + ab * A_BYTES + HALF_BYTES, &mapA, KHALF, qt * BM, A_FULL(ab));
         for (int p = p0; p < p1; ++p) {
           const int st = it % F_STAGES, rd = it / F_STAGES;
           if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
           const uint32_t dst = s0 + F_B_OFF + st * B_TILE;
           const int row = p * a.dstride * TN;
-          mbar_expect_tx(FULL(st), B_HALF + TN * a.hi_cols * 2);
-          tma_load_2d(dst, &mapB, 0, row, FULL(st));
-          tma_load_2d(dst + B_HALF, &mapBhi, KHALF, row, FULL(st));
+          if (F8) {
+            mbar_expect_tx(FULL(st), B_TILE);
+            tma_load_2d(dst, &mapB, 0, row, FULL(st));
+          } else {
+            mbar_expect_tx(FULL(st), B_HALF + TN * a.hi_cols * 2);
+            tma_load_2d(dst, &mapB, 0, row, FULL(st));
+            tma_load_2d(dst + B_HALF, &mapBhi, KHALF, row, FULL(st));
+          }
           ++it;
         }
       }
@@ -191,8 +209,12 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           const int st = it % F_STAGES, rd = it / F_STAGES;
           if (!mbar_wait(FULL(st), rd & 1, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          umma_tile<TN>(tmem + (uint32_t)(b * TN), s0 + F_A_OFF + ab * TILE_BYTES, s0 + F_B_OFF + st * B_TILE,
-                        a.ksteps);
+          if (F8)
+            umma_tile_e4m3<TN>(tmem + (uint32_t)(b * TN), s0 + F_A_OFF + ab * A_BYTES, s0 + F_B_OFF + st * B_TILE,
+                               a.ksteps);
+          else
+            umma_tile<TN>(tmem + (uint32_t)(b * TN), s0 + F_A_OFF + ab * A_BYTES, s0 + F_B_OFF + st * B_TILE,
+                          a.ksteps);
           umma_commit(EMPTY(st));
           umma_commit(ACC_FULL(b));
           ++it;
@@ -459,7 +481,7 @@ __global__ void merge_fallback_kernel(const uint64_t* __restrict__ part, const i
   }
 }
 
-template <int MODE, int GW>
+template <int MODE, int GW, bool F8>
 void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, FilterArgs a, const char* name,
                 cudaStream_t s) {
   // chunk size: long enough to amortise the query-tile switch (at most 32 tiles), short
@@ -470,10 +492,11 @@ void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap&
   a.NCH = ceil_div(a.NP, a.CH);
   const int U = a.NCH * a.QT;
   const int grid = std::min(G, U);
-  auto kern = tc_filter_kernel<MODE, GW>;
-  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, F_SMEM));
+  auto kern = tc_filter_kernel<MODE, GW, F8>;
+  constexpr int smem = FLayout<F8>::SMEM;
+  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   ProfScope _ps(name, s);
-  kern<<<grid, F_THREADS, F_SMEM, s>>>(ma, mb, mbhi, a);
+  kern<<<grid, F_THREADS, smem, s>>>(ma, mb, mbhi, a);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
@@ -512,11 +535,13 @@ FilterPlan plan_filter(int64_t n, int CT) {
 
 void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, int hi_cols,
                         const FilterPlan& plan, int nq, int64_t n, int d, int QT, int CT, float* tau, int* cnt,
-                        uint64_t* cand, int* err, cudaStream_t s) {
+                        uint64_t* cand, int* err, bool e4m3, cudaStream_t s) {
   FilterArgs a{};
   a.hi_cols = hi_cols;
   a.nq = nq;
-  a.ksteps = tc_ksteps(d);
+  a.ksteps = e4m3 ? tc_ksteps_e4m3(d) : tc_ksteps(d);
+  // scores of E4M3 codes carry the factor kE4M3Scale^2
+  const float margin = e4m3 ? kTauMargin * kE4M3Scale * kE4M3Scale : kTauMargin;
   a.n = n;
   a.QT = QT;
   a.err = err;
@@ -526,11 +551,16 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
     a.dstride = plan.S;
     a.gmax = gmax.ptr;
     a.M = plan.M;
-    if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64>(ma, mb, mbhi, a, "tc_prepass", s);
-    else run_filter<MODE_GROUPMAX, 8>(ma, mb, mbhi, a, "tc_prepass", s);
+    if (e4m3) {
+      if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64, true>(ma, mb, mbhi, a, "tc_prepass", s);
+      else run_filter<MODE_GROUPMAX, 8, true>(ma, mb, mbhi, a, "tc_prepass", s);
+    } else {
+      if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64, false>(ma, mb, mbhi, a, "tc_prepass", s);
+      else run_filter<MODE_GROUPMAX, 8, false>(ma, mb, mbhi, a, "tc_prepass", s);
+    }
     {
       ProfScope _ps("tc_tau_select", s);
-      tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, kTauMargin, tau);
+      tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, margin, tau);
       count_launch();
       LSHG_CHECK_LAUNCH();
     }
@@ -543,7 +573,8 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
   a.cnt = cnt;
   a.cand = cand;
   a.cap = plan.cap;
-  run_filter<MODE_FILTER, 64>(ma, mb, mbhi, a, "tc_filter", s);
+  if (e4m3) run_filter<MODE_FILTER, 64, true>(ma, mb, mbhi, a, "tc_filter", s);
+  else run_filter<MODE_FILTER, 64, false>(ma, mb, mbhi, a, "tc_filter", s);
 }
 
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,

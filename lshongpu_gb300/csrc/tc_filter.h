@@ -32,8 +32,11 @@ FilterPlan plan_filter(int64_t n, int CT);
 // Prepass + threshold selection + filter pass: fills cnt[q] and cand[q][0..cap).
 // mb: base tiles (256 rows x 64 columns boxes); mbhi: boxes of the second 64-column half
 // trimmed to hi_cols columns (the K steps past the data dimension are never read).
+// e4m3: operands are E4M3 codes (rows of 128 bytes; mb boxes of 256 rows x 128 bytes, mbhi
+// unused); otherwise BF16 as above.
 void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& mbhi, int hi_cols,
-                        const FilterPlan& plan, int nq, int64_t n, int d, int QT, int CT, float* tau, int* cnt, uint64_t* cand, int* err, cudaStream_t s);
+                        const FilterPlan& plan, int nq, int64_t n, int d, int QT, int CT, float* tau, int* cnt,
+                        uint64_t* cand, int* err, bool e4m3, cudaStream_t s);
 
 // Top-CT keys a query from its survivors; overflowed queries are listed in ovf.
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,

@@ -130,6 +130,38 @@ __device__ __forceinline__ void umma_tile(uint32_t d_tmem, uint32_t a_base, uint
   }
 }
 __host__ __device__ inline int tc_ksteps(int d) { return d <= 0 ? 1 : (d > KD ? KD / 16 : (d + 15) / 16); }
+
+// FP8 operands: rows of KD E4M3 bytes (one 128-byte swizzle row holds the whole K).
+// Instruction descriptor: kind::f8f6f4, A = B = E4M3 (format 0), D = F32, K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void umma_e4m3(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// One 128 x N x (32 * ksteps) E4M3 product: each step advances 32 bytes (K = 32) along the
+// single 128-byte row of A (128-row tile) and B (N-row tile); as with BF16, rows are zero
+// past d, so ksteps = ceil(d / 32) gives the same sums as all four steps.
+template <int N>
+__device__ __forceinline__ void umma_tile_e4m3(uint32_t d_tmem, uint32_t a_base, uint32_t b_base, int ksteps) {
+  constexpr uint32_t idesc = idesc_e4m3(BM, N);
+#pragma unroll
+  for (int kk = 0; kk < KD / 32; ++kk) {
+    if (kk < ksteps) {
+      const uint32_t koff = kk * 32;
+      umma_e4m3(d_tmem, smem_desc(a_base + koff), smem_desc(b_base + koff), idesc, kk > 0 ? 1u : 0u);
+    }
+  }
+}
+__host__ __device__ inline int tc_ksteps_e4m3(int d) { return d <= 0 ? 1 : (d > KD ? KD / 32 : (d + 31) / 32); }
+// E4M3 codes hold unit vectors times this factor: every component (|v| <= 1) stays within
+// the format's range (448) and components down to 2^-14 stay in its normal range.
+constexpr float kE4M3Scale = 256.0f;
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -181,6 +213,8 @@ __device__ __forceinline__ float max8(const uint32_t (&v)[64], int g) {
 // Tensor map over `rows` bf16 rows of KD elements; boxes of 64 columns x box_rows rows
 // with 128-byte swizzle (the layout smem_desc describes).
 CUtensorMap make_map(const void* base, int64_t rows, int box_rows = BM, int box_cols = KHALF);
+// Rows of KD E4M3 bytes; boxes of box_rows rows x 128 bytes with 128-byte swizzle.
+CUtensorMap make_map_e4m3(const void* base, int64_t rows, int box_rows);
 
 }  // namespace tc
 }  // namespace lshg

@@ -35,6 +35,8 @@
 #include "tc_filter.h"
 #include "tc_ptx.cuh"
 
+#include <cuda_fp8.h>
+
 namespace lshg {
 
 void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
@@ -390,6 +392,33 @@ __global__ void to_unit_bf16_kernel(const float* __restrict__ x, int64_t n, int 
   }
 }
 
+// Unit rows as E4M3 codes of (x / |x|) * kE4M3Scale, KD bytes a row, zero padded.
+__global__ void to_unit_e4m3_kernel(const float* __restrict__ x, int64_t n, int d, int64_t rows_pad,
+                                    uint8_t* __restrict__ out) {
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < rows_pad; i += nw) {
+    float ss = 0.0f;
+    if (i < n)
+      for (int j = lane; j < d; j += 32) ss = fmaf(x[i * d + j], x[i * d + j], ss);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    const float inv = ss > 0.0f ? rsqrtf(ss) * kE4M3Scale : 0.0f;
+    for (int j = lane; j < KD; j += 32) {
+      const float v = (i < n && j < d) ? x[i * d + j] * inv : 0.0f;
+      out[i * KD + j] = (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+    }
+  }
+}
+
+void to_unit_e4m3(const float* x, int64_t n, int d, int64_t rows_pad, uint8_t* out, cudaStream_t s) {
+  int blocks = (int)std::min<int64_t>((rows_pad * 32 + 255) / 256, (int64_t)num_sms() * 16);
+  to_unit_e4m3_kernel<<<std::max(blocks, 1), 256, 0, s>>>(x, n, d, rows_pad, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
 void to_unit_bf16(const float* x, int64_t n, int d, int64_t rows_pad, uint16_t* out, cudaStream_t s) {
   int64_t warps = rows_pad;
   int blocks = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms() * 16);
@@ -430,6 +459,21 @@ CUtensorMap make_map(const void* base, int64_t rows, int box_rows, int box_cols)
   return m;
 }
 
+CUtensorMap make_map_e4m3(const void* base, int64_t rows, int box_rows) {
+  LSHG_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
+  LSHG_REQUIRE(box_rows >= 1 && box_rows <= 256, "TMA box rows must be in [1, 256]");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {(cuuint64_t)KD, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)KD};
+  cuuint32_t box[2] = {(cuuint32_t)KD, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(LSHG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
 namespace {
 
 template <int STAGES, int CT>
@@ -454,14 +498,19 @@ void tc_prepare(Index& I, cudaStream_t s) {
   const int64_t npad = (int64_t)ceil_div(I.n, FILTER_TN) * FILTER_TN;  // whole filter tiles
   I.xbf.alloc((size_t)npad * KD, s);
   to_unit_bf16(I.x.ptr, I.n, I.d, npad, I.xbf.ptr, s);
+  if (I.p.implementation == 9) {  // E4M3 operands for the filter (BF16 stays for the fallback)
+    I.xf8.alloc((size_t)npad * KD, s);
+    to_unit_e4m3(I.x.ptr, I.n, I.d, npad, I.xf8.ptr, s);
+  }
 }
 
 void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
   using namespace tc;
   if (nq <= 0) return;
   LSHG_REQUIRE(k <= 128, "tensor-core scan: k must be <= 128");
-  // candidates re-ranked a query: at least twice k up to k = 64 (BF16 scores can swap
-  // near-equal neighbours at the boundary); 128 (the list kernel's maximum) beyond
+  // candidates re-ranked a query: at least twice k up to k = 64 (BF16 or E4M3 scores can
+  // swap near-equal neighbours at the boundary); 128 (the list kernel's maximum) beyond
+  const bool e4m3 = I.p.implementation == 9;
   const int CT = k <= 32 ? 64 : 128;
   const int64_t qpad = (int64_t)ceil_div(nq, BM) * BM;
   const int QT = (int)(qpad / BM);
@@ -480,6 +529,14 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   // the filter's second 64-column half only up to the last K step (columns 64..16*ksteps)
   const int hi_cols = std::max(8, std::min(KHALF, 16 * tc_ksteps(I.d) - KHALF));
   const CUtensorMap mb256hi = make_map(I.xbf.ptr, npad, FILTER_TN, hi_cols);
+  DevBuf<uint8_t> qf8;
+  CUtensorMap ma8{}, mb8{};
+  if (e4m3) {
+    qf8.alloc((size_t)qpad * KD, s);
+    to_unit_e4m3(q, nq, I.d, qpad, qf8.ptr, s);
+    ma8 = make_map_e4m3(qf8.ptr, qpad, BM);
+    mb8 = make_map_e4m3(I.xf8.ptr, npad, FILTER_TN);
+  }
 
   // 1-2. thresholds and survivors
   DevBuf<float> tau((size_t)nq, s);
@@ -487,7 +544,12 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   int* ovf = cnt.ptr + nq;
   LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, (size_t)(nq + 1) * sizeof(int), s));
   DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
-  launch_filter_scan(ma, mb256, mb256hi, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, s);
+  if (e4m3)
+    launch_filter_scan(ma8, mb8, mb8, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, true,
+                       s);
+  else
+    launch_filter_scan(ma, mb256, mb256hi, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr,
+                       false, s);
 
   // 3. top-CT of the survivors
   DevBuf<uint64_t> best((size_t)nq * CT, s);

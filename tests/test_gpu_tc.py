@@ -132,3 +132,51 @@ def test_tc_edge_shapes(engine, orc, n, nq, k, d):
         assert np.all(res["distance"][:, n:] == np.float32(2.0 ** 31))
     a, b = _query_both_paths(idx, q, k)
     assert np.array_equal(a["ID"], b["ID"]) and np.array_equal(a["distance"], b["distance"])
+
+
+# ---- E4M3 (FP8) tensor-core scores (implementation 9) ------------------------------------
+# Tolerance stated: recall@k >= 0.98 against the exact FP32 scan (E4M3 keeps 3 mantissa
+# bits, so more near-equal neighbours trade places at the candidate boundary than with
+# BF16; 128 candidates are re-ranked a query), and every returned distance equals the
+# oracle's FP32 distance for that id bit for bit (the re-rank is the same FP32 code).
+
+
+@pytest.mark.parametrize("n,nq,k,d", [(1000, 200, 32, 100), (20000, 300, 32, 100), (6000, 129, 100, 100),
+                                      (70000, 200, 10, 64), (3000, 5, 64, 37), (9000, 130, 32, 128)])
+def test_tc_fp8_recall_and_exact_distances(engine, orc, n, nq, k, d):
+    x = datasets.clustered(n, d, 161, count=40)
+    q = datasets.clustered(nq, d, 162, count=40)
+    idx = engine.Index(x, implementation=engine.IMPL_TC_FP8, distanceFunc=1)
+    res = idx.query(q, k)
+    kk = min(k, n)
+    ids, ds = orc.exact_topk(x, q, kk, dist=1)
+    rec = recall(res["ID"][:, :kk], ids)
+    assert rec >= 0.98, f"E4M3 recall@{kk} = {rec:.4f}"
+    lookup = [dict(zip(i.tolist(), dd.tolist())) for i, dd in zip(ids, ds)]
+    for qi in range(nq):
+        for rid, rd in zip(res["ID"][qi], res["distance"][qi]):
+            if rid in lookup[qi]:
+                assert np.float32(rd) == np.float32(lookup[qi][rid])
+    for row in res:
+        keys = [(dd, i) for i, dd in zip(row["ID"], row["distance"]) if i >= 0]
+        assert keys == sorted(keys)
+
+
+def test_tc_fp8_overflow_and_persistence(engine, orc, tmp_path):
+    """Tied duplicates send a query through the (BF16) list-kernel fallback while the rest
+    of the batch stays on the E4M3 filter; a saved and reloaded E4M3 index answers the same."""
+    n = 20000
+    x = datasets.clustered(n, D, 171, count=40)
+    x[1000:6000] = x[777]
+    q = datasets.clustered(48, D, 172, count=40)
+    q[5] = x[777]
+    idx = engine.Index(x, implementation=engine.IMPL_TC_FP8, distanceFunc=1)
+    res = idx.query(q, 32)
+    ids, ds = orc.exact_topk(x, q, 32, dist=1)
+    assert res["ID"][5].tolist() == ids[5].tolist()
+    assert np.array_equal(res["distance"][5], ds[5])
+    assert recall(res["ID"], ids) >= 0.98
+    p = str(tmp_path / "fp8.idx")
+    idx.save(p)
+    again = engine.Index.load(p).query(q, 32)
+    assert np.array_equal(again, res)
