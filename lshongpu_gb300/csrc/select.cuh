@@ -182,11 +182,42 @@ __device__ __forceinline__ void topc_push(TopCShared s, int q, uint64_t key, uin
 // when limit < 0).  Block-wide: all threads call it; warps take queries round-robin.
 // Returns after a __syncthreads so new thresholds are visible.
 // kRegSort: fold with warp_fold_buffer_regs.
+// Block-cooperative warp_fold_buffer: every thread of the block takes part (same result).
+__device__ __forceinline__ void block_fold_buffer(uint64_t* kept, int C, uint64_t* buf, int cnt) {
+  const int nb = next_pow2_dev(cnt < 2 ? 2 : cnt);
+  for (int i = cnt + threadIdx.x; i < nb; i += blockDim.x) buf[i] = kEmptyKey;
+  __syncthreads();
+  block_bitonic_sort(buf, nb);
+  for (int i = threadIdx.x; i < C; i += blockDim.x) {
+    const int j = C - 1 - i;
+    const uint64_t b = (j < nb) ? buf[j] : kEmptyKey;
+    if (b < kept[i]) kept[i] = b;
+  }
+  __syncthreads();
+  block_bitonic_merge(kept, C);
+}
+
 template <bool kRegSort = false>
 __device__ __forceinline__ void topc_flush(TopCShared s, int nq, int limit) {
   __syncthreads();
   const int warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
+  if (s.C >= 512 && nq * 4 <= nwarps) {
+    // long lists and few queries a block: one warp per query would leave most of the
+    // block waiting on a C-key merge, so the whole block folds each query in turn
+    for (int q = 0; q < nq; ++q) {
+      const int c = s.cnt[q];  // read by every thread before the fold's first barrier
+      if (c > limit && c > 0) {
+        block_fold_buffer(s.kept + (size_t)q * s.C, s.C, s.buf + (size_t)q * s.B, c);
+        if (threadIdx.x == 0) {
+          s.cnt[q] = 0;
+          s.thr[q] = s.kept[(size_t)q * s.C + s.C - 1];
+        }
+      }
+    }
+    __syncthreads();
+    return;
+  }
   for (int q = warp; q < nq; q += nwarps) {
     int c = s.cnt[q];
     if (c > limit && c > 0) {
