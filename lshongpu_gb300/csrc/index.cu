@@ -24,6 +24,12 @@ int next_pow2(int v) {
   return p;
 }
 
+void tile_sketches(Index& I, cudaStream_t s) {
+  const int64_t tiles = (I.n + 127) / 128;
+  I.xst.alloc((size_t)tiles * 128 * I.wp, s);
+  launch_tile_sketches(I.xs.ptr, I.n, I.wp, I.xst.ptr, s);
+}
+
 void launch_pack_bytes(const uint8_t* in, int64_t n, int sbytes, uint32_t* out, int wp, uint8_t pad, cudaStream_t s);
 size_t wmh_state_bytes();
 size_t lsh_query_smem(const LshQueryArgs& a);
@@ -242,7 +248,7 @@ Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
   x.release(); xnorm.release(); xt.release(); xs.release(); xsf.release(); xsft.release(); sk_planes.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
-  xbf.release(); xbf_scale.release(); xf8.release(); qerr.release(); qstats.release();
+  xbf.release(); xbf_scale.release(); xf8.release(); xst.release(); qerr.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();
@@ -410,6 +416,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
       launch_tile_transpose(I.xsf.ptr, n, I.sdim, I.xsft.ptr, s);
     } else {
       I.xs = std::move(packed);
+      if (p.framework == 0) tile_sketches(I, s);
     }
   }
 
@@ -533,7 +540,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     splits = scan_bits_splits(I.n, nq, C);
     part.alloc((size_t)nq * splits * C, s);
     int op = impl == 3 ? OP_HAMMING : (impl == 4 ? OP_BYTE_JACCARD : OP_ONEBIT_JACCARD);
-    launch_scan_bits(I.xs.ptr, I.n, I.wp, I.words, I.sbytes, qs.ptr, nq, op, C, splits, part.ptr, s);
+    launch_scan_bits(I.xst.ptr, I.n, I.wp, I.words, I.sbytes, qs.ptr, nq, op, C, splits, part.ptr, s);
   }
   const uint64_t* cand = part.ptr;
   DevBuf<uint64_t> merged;

@@ -53,6 +53,7 @@ struct Index {
   int sk_kind = 0;
   int words = 0, wp = 0, sbytes = 0, sdim = 0;
   DevBuf<uint32_t> xs;       // packed sketches, rows of wp words
+  DevBuf<uint32_t> xst;      // linear scans: the same, tiled [ceil(N/128)][wp/4][128] x 16 B
   DevBuf<float> xsf, xsft;   // JL sketches [n][sdim] and their tile layout
   DevBuf<float> sk_planes;   // SimHash planes [32*sketchDim][d] or JL rows [sdim][d]
   WmhState wmh_sk;
@@ -104,6 +105,9 @@ void sketch_queries(Index& idx, float* q, int nq, DevBuf<uint32_t>* qs, DevBuf<f
                     DevBuf<uint16_t>* qkeys, cudaStream_t stream);
 
 int next_pow2(int v);
+
+// Build idx.xst (the linear scans' tiled sketches) from idx.xs.
+void tile_sketches(Index& idx, cudaStream_t stream);
 
 // Persistence (persist.cpp): checksummed binary image of a built index.
 void save_index(const Index& idx, const char* path);

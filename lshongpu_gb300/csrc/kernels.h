@@ -74,8 +74,12 @@ int scan_float_splits(int64_t n, int nq, int C);
 // ---- scan_bits.cu ----------------------------------------------------------------
 // Top-C keys per (query, split) over packed sketches: rows of wp 32-bit words
 // (wp % 4 == 0) holding `words` real words (bytes for OP_BYTE_JACCARD: `sbytes` real).
-int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs,
+// xst: sketches tiled by launch_tile_sketches ([ceil(n/128)][wp/4][128] 16-byte chunks).
+int launch_scan_bits(const uint32_t* xst, int64_t n, int wp, int words, int sbytes, const uint32_t* qs,
                      int nq, int op, int C, int splits, uint64_t* out, cudaStream_t s);
+// Rows of wp words ([n][wp], wp % 4 == 0) -> the scans' tiled layout: chunk c (16 bytes)
+// of point t*128 + l at [t][c][l]; points past n are zero.
+void launch_tile_sketches(const uint32_t* xs, int64_t n, int wp, uint32_t* xst, cudaStream_t s);
 int scan_bits_splits(int64_t n, int nq, int C);
 
 // ---- rerank.cu -------------------------------------------------------------------

@@ -197,6 +197,7 @@ std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
     read_ops(r, I.ops_keys, s);
     read_ops(r, I.ops_sketch, s);
     buffers_io(r, I, s);
+    if (I.p.framework == 0 && I.xs.n) tile_sketches(I, s);  // derived layout, not stored
     uint64_t want = r.h, got = 0;
     if (fread(&got, 1, 8, f) != 8 || got != want) throw Error(LSHG_ERR_IO, "index file checksum mismatch");
   } catch (...) {

@@ -6,9 +6,11 @@
 //   one-bit WMH    1 - sum(32 - popc(q ^ x)) / (32 * words)         (:118-134)
 //   byte WMH       1 - (#equal bytes) / sketchDim                   (:102-116)
 // GB300 form: a CTA owns QB queries (sketches in shared memory) and a split of the
-// base; each thread holds one point's sketch in registers (loaded with 128-bit,
-// coalesced loads) and scores it against its half of the CTA's queries with XOR and
-// popcount.  Candidates are filtered against each query's running threshold and
+// base; each thread holds one point's sketch in registers and scores it against its half
+// of the CTA's queries with XOR and popcount.  The base is read in the tiled layout
+// (chunk c of point t*128 + l at [t][c][l], 16 bytes a chunk), so one warp load of a
+// chunk is 512 contiguous bytes; read as rows, 32 lanes a row apart would touch 32 lines
+// an instruction and the L1 data pipe, not the integer ALU, would bound the scan.  Candidates are filtered against each query's running threshold and
 // folded into a per-query sorted top-C list (select.cuh).
 #include "common.cuh"
 #include "kernels.h"
@@ -66,7 +68,7 @@ __device__ __forceinline__ int word_score(uint32_t a, uint32_t b) {
 // NC > 0: rows of exactly NC 128-bit chunks, loops fully unrolled without bounds tests;
 // NC = 0: any row width up to kMaxChunks chunks (runtime bound).
 template <int OP, int QB, int KBUF, int T, int NC>
-__global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __restrict__ xs, int64_t n, int wp, int words,
+__global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __restrict__ xst, int64_t n, int wp, int words,
                                                         int sbytes, const uint32_t* __restrict__ qs, int nq, int C,
                                                         int tiles_per_split, int splits, uint64_t* __restrict__ out) {
   static_assert(KBUF >= T * kTile, "append buffer must absorb T tiles");
@@ -106,9 +108,9 @@ __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __res
     const int64_t p = (int64_t)tile * kTile + pl;
     const bool valid = p < n;
     uint4 xr[NCH];
-    const uint4* row = reinterpret_cast<const uint4*>(xs + (valid ? p : 0) * wp);
+    const uint4* col = reinterpret_cast<const uint4*>(xst) + (int64_t)tile * nc * kTile + pl;
 #pragma unroll
-    for (int c = 0; c < NCH; ++c) xr[c] = ((NC > 0 || c < nc) && valid) ? __ldg(&row[c]) : make_uint4(0, 0, 0, 0);
+    for (int c = 0; c < NCH; ++c) xr[c] = (NC > 0 || c < nc) ? __ldg(&col[c * kTile]) : make_uint4(0, 0, 0, 0);
 
     if (valid) {
 #pragma unroll
@@ -218,6 +220,28 @@ int scan_bits_splits(int64_t n, int nq, int C) {
     }
   }
   return best;
+}
+
+__global__ void tile_sketches_kernel(const uint4* __restrict__ xs, int64_t n, int nc, int64_t total,
+                                     uint4* __restrict__ xst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = i % kTile, tc = i / kTile;   // i = (tile * nc + c) * kTile + l
+    const int64_t c = tc % nc, t = tc / nc;
+    const int64_t p = t * kTile + l;
+    xst[i] = p < n ? xs[p * nc + c] : make_uint4(0, 0, 0, 0);
+  }
+}
+
+void launch_tile_sketches(const uint32_t* xs, int64_t n, int wp, uint32_t* xst, cudaStream_t s) {
+  LSHG_REQUIRE(wp % 4 == 0, "sketch rows must be a multiple of 4 words");
+  const int nc = wp / 4;
+  const int64_t total = (n + kTile - 1) / kTile * kTile * nc;
+  if (total == 0) return;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
+  tile_sketches_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const uint4*>(xs), n, nc, total,
+                                              reinterpret_cast<uint4*>(xst));
+  count_launch();
+  LSHG_CHECK_LAUNCH();
 }
 
 int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int op,
