@@ -201,11 +201,14 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
 // Register-blocked variant for C <= 128 (k <= 128): 64 queries a CTA, warp w owns
 // queries 8w .. 8w+7 and lane l points 4l .. 4l+3 of each 128-point tile, so a thread
 // keeps an 8 x 4 micro-tile (32 FMAs per dimension step for three shared loads).  A
-// query's top-C list lives in shared memory and is touched only when some candidate of
-// the tile beats the query's threshold (one warp vote); there is no block-level selection
+// query's top-C list lives in shared memory; candidates that beat the query's threshold
+// (one warp vote a tile) are appended to its 64-key buffer and merged into the list only
+// when the buffer fills -- in a short split nearly every tile brings a candidate, and a
+// merge a tile would cost more than the tile's FMAs.  There is no block-level selection
 // protocol and no barrier besides the tile copy's.
 // ---------------------------------------------------------------------------------
 constexpr int kRegQB = 64;
+constexpr int kRegBuf = 64;  // candidate keys a query buffers before a merge
 
 __host__ __device__ inline size_t reg_scan_smem(int d, int C, int nbuf) {
   size_t off = 0;
@@ -214,7 +217,33 @@ __host__ __device__ inline size_t reg_scan_smem(int d, int C, int nbuf) {
   smem_take(off, (size_t)kRegQB * 4);            // query magnitudes
   smem_take(off, (size_t)kRegQB * C * 8);        // top-C lists
   smem_take(off, (size_t)8 * 32 * 8);            // per-warp scratch
+  smem_take(off, (size_t)kRegQB * kRegBuf * 8);  // candidate buffers
   return off;
+}
+
+// Merge a query's buffered candidates (cnt <= kRegBuf keys, all below the list's
+// threshold when they were added) into its sorted list of C = 32*EC keys; returns the new
+// threshold.  Executed by the whole warp.
+template <int EC>
+__device__ __noinline__ uint64_t fold_candidates(uint64_t* list, const uint64_t* buf, int cnt) {
+  const int lane = threadIdx.x & 31;
+  uint64_t y[2] = {lane < cnt ? buf[lane] : kEmptyKey, lane + 32 < cnt ? buf[lane + 32] : kEmptyKey};
+  warp_bitonic<2>(y, lane, false);  // element e*32 + lane, ascending
+  uint64_t x[EC];
+#pragma unroll
+  for (int e = 0; e < EC; ++e) x[e] = e < 2 ? y[e] : kEmptyKey;  // the 32*EC smallest, ascending
+  uint64_t best[EC];
+#pragma unroll
+  for (int e = 0; e < EC; ++e) best[e] = list[e * 32 + lane];
+#pragma unroll
+  for (int e = 0; e < EC; ++e) {
+    const uint64_t r = __shfl_sync(0xffffffffu, x[EC - 1 - e], 31 - lane);
+    best[e] = best[e] < r ? best[e] : r;
+  }
+  warp_bitonic<EC>(best, lane, true);
+#pragma unroll
+  for (int e = 0; e < EC; ++e) list[e * 32 + lane] = best[e];
+  return __shfl_sync(0xffffffffu, best[EC - 1], 31);
 }
 
 // Merge one query's candidates (k0..k3 on every lane: 128 keys, only those below `thr`
@@ -281,6 +310,7 @@ __global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
   float* qn = reinterpret_cast<float*>(smem + smem_take(off, (size_t)kRegQB * 4));
   uint64_t* lists = reinterpret_cast<uint64_t*>(smem + smem_take(off, (size_t)kRegQB * C * 8));
   uint64_t* scratch = reinterpret_cast<uint64_t*>(smem + smem_take(off, (size_t)8 * 32 * 8));
+  uint64_t* cbuf = reinterpret_cast<uint64_t*>(smem + smem_take(off, (size_t)kRegQB * kRegBuf * 8));
 
   const int q0 = blockIdx.x * kRegQB;
   const int split = blockIdx.y;
@@ -298,8 +328,13 @@ __global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
   for (int i = threadIdx.x; i < kRegQB * C; i += blockDim.x) lists[i] = kEmptyKey;
   __syncthreads();  // lists are read by their owning warps (and written out even for an empty split)
   uint64_t thr[8];
+  int bcnt[8];  // buffered candidates a query (warp-uniform)
 #pragma unroll
-  for (int a = 0; a < 8; ++a) thr[a] = kEmptyKey;
+  for (int a = 0; a < 8; ++a) {
+    thr[a] = kEmptyKey;
+    bcnt[a] = 0;
+  }
+  const unsigned lt_mask = (1u << lane) - 1u;
 
   const int tile_f4 = kTile * d / 4;
   auto slot = [&](int tile) { return nbuf == 2 ? (tile & 1) : 0; };
@@ -360,8 +395,39 @@ __global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
       for (int b = 0; b < 4; ++b)
         k[b] = (pbase + b < n) ? make_key(finish_distance<DIST>(acc[a][b], acc2[a][b], qn[qi], xn[b]), (int)(pbase + b))
                                : kEmptyKey;
-      if (__any_sync(0xffffffffu, k[0] < thr[a] || k[1] < thr[a] || k[2] < thr[a] || k[3] < thr[a]))
-        thr[a] = merge_candidates<EC>(lists + (size_t)qi * C, k[0], k[1], k[2], k[3], thr[a], scratch + w * 32);
+      if (!__any_sync(0xffffffffu, k[0] < thr[a] || k[1] < thr[a] || k[2] < thr[a] || k[3] < thr[a])) continue;
+      uint64_t* qbuf = cbuf + (size_t)qi * kRegBuf;
+      unsigned m[4];
+      int nc = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        m[b] = __ballot_sync(0xffffffffu, k[b] < thr[a]);
+        nc += __popc(m[b]);
+      }
+      if (bcnt[a] + nc > kRegBuf) {
+        if (bcnt[a] > 0) {  // make room: merge the buffer, then re-filter with the new threshold
+          thr[a] = fold_candidates<EC>(lists + (size_t)qi * C, qbuf, bcnt[a]);
+          bcnt[a] = 0;
+          nc = 0;
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            m[b] = __ballot_sync(0xffffffffu, k[b] < thr[a]);
+            nc += __popc(m[b]);
+          }
+        }
+        if (nc > kRegBuf) {  // more than a buffer's worth in one tile: merge them directly
+          thr[a] = merge_candidates<EC>(lists + (size_t)qi * C, k[0], k[1], k[2], k[3], thr[a], scratch + w * 32);
+          continue;
+        }
+      }
+      int pos = bcnt[a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        if (m[b] & (1u << lane)) qbuf[pos + __popc(m[b] & lt_mask)] = k[b];
+        pos += __popc(m[b]);
+      }
+      bcnt[a] = pos;
+      __syncwarp();
     }
     __syncthreads();  // every read of this tile's buffer is done: the next copy may reuse it
   }
@@ -370,6 +436,7 @@ __global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
   for (int a = 0; a < 8; ++a) {
     const int qi = 8 * w + a;
     if (q0 + qi >= nq) continue;
+    if (bcnt[a] > 0) fold_candidates<EC>(lists + (size_t)qi * C, cbuf + (size_t)qi * kRegBuf, bcnt[a]);
 #pragma unroll
     for (int e = 0; e < EC; ++e)
       out[((int64_t)(q0 + qi) * splits + split) * C + e * 32 + lane] = lists[(size_t)qi * C + e * 32 + lane];
