@@ -383,18 +383,31 @@ __global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
         }
     }
     const int64_t pbase = (int64_t)tile * kTile + 4 * lane;
-    float xn[4];
+    float xn[4], xinv[4];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) xn[b] = (DIST == DIST_ANGULAR && pbase + b < n) ? xnorm[pbase + b] : 1.0f;
+    for (int b = 0; b < 4; ++b) {
+      xn[b] = (DIST == DIST_ANGULAR && pbase + b < n) ? xnorm[pbase + b] : 1.0f;
+      xinv[b] = __frcp_rn(xn[b]);
+    }
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
       const int qi = 8 * w + a;
       if (q0 + qi >= nq) continue;  // warp-uniform
+      // Angular pre-filter: 1 - dot * (1/|q|) * (1/|x|) is within ~5e-7 of the exact
+      // 1 - dot / (|q| |x|), so a pair whose estimate exceeds the threshold's distance by
+      // more than 1e-5 cannot enter the list and skips the exact divide; NaN or infinite
+      // estimates (zero norms) and an empty list (NaN threshold) always take the exact path.
+      const float bound = key_dist(thr[a]) + 1e-5f;
+      const float qinv = __frcp_rn(qn[qi]);
       uint64_t k[4];
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
-        k[b] = (pbase + b < n) ? make_key(finish_distance<DIST>(acc[a][b], acc2[a][b], qn[qi], xn[b]), (int)(pbase + b))
-                               : kEmptyKey;
+      for (int b = 0; b < 4; ++b) {
+        k[b] = kEmptyKey;
+        if (pbase + b < n) {
+          const bool skip = DIST == DIST_ANGULAR && __fmaf_rn(-acc[a][b], __fmul_rn(qinv, xinv[b]), 1.0f) > bound;
+          if (!skip) k[b] = make_key(finish_distance<DIST>(acc[a][b], acc2[a][b], qn[qi], xn[b]), (int)(pbase + b));
+        }
+      }
       if (!__any_sync(0xffffffffu, k[0] < thr[a] || k[1] < thr[a] || k[2] < thr[a] || k[3] < thr[a])) continue;
       uint64_t* qbuf = cbuf + (size_t)qi * kRegBuf;
       unsigned m[4];
