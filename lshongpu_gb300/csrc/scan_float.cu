@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
     for (int a = 0; a < 8; ++a)
 #pragma unroll
       for (int b = 0; b < 4; ++b) { acc[a][b] = 0.0f; acc2[a][b] = 0.0f; }
+#pragma unroll 4
     for (int j = 0; j < d; ++j) {
       const float4 xv = *reinterpret_cast<const float4*>(&xcur[j * kTile + 4 * lane]);
       const float4 qa0 = *reinterpret_cast<const float4*>(&qs[j * kRegQB + 8 * w]);
