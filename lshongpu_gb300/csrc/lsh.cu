@@ -29,7 +29,7 @@ namespace {
 constexpr int kQThreads = 256;
 constexpr int kQBuf = 2 * kQThreads;
 constexpr int kMaxTables = 256;
-constexpr int kUnroll = 4;                    // bucket entries a thread loads per round
+constexpr int kUnroll = 8;                    // bucket entries a thread loads per round
 constexpr int kRound = kUnroll * kQThreads;   // entries walked per round
 constexpr int kScoreAt = 1024;                // score the distinct list once it holds this many
 constexpr int kListCap = kScoreAt + kRound;   // a round adds at most kRound ids
@@ -110,14 +110,6 @@ __device__ __forceinline__ float sketch_distance(const LshQueryArgs& a, int id, 
   return __fsub_rn(1.0f, __fdiv_rn((float)(32 * a.words - acc), (float)(32 * a.words)));
 }
 
-// Dedupe of one query's bucket entries on the CTA's bitmap (one bit a base point): the
-// thread whose atomicOr sets an id's bit reports it new, so every distinct id is reported
-// exactly once.  (A shared-memory id set in front of the bitmap measured slower once
-// rows were staged: its 32 KB cost more resident CTAs than it saved in L2 atomics.)
-__device__ __forceinline__ bool dedupe_new(uint32_t* bitmap, int id) {
-  const uint32_t bit = 1u << (id & 31);
-  return !(atomicOr(&bitmap[id >> 5], bit) & bit);
-}
 
 
 // Bounded wait on a staging barrier; on timeout raises error 3 (when err is given).
@@ -209,7 +201,7 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   TopCShared S{kept, buf, &cnt_s, &thr_s, a.C, kQBuf};
   __shared__ __align__(8) uint64_t stage_bar[NW];
   uint32_t* bitmap = a.bitmaps + (int64_t)blockIdx.x * ((a.n + 31) / 32);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
   unsigned char* stage_w = smem + (uint32_t)((tid >> 5) * kStageRows) * stage_slot;
   const uint32_t bar_w = tc::smem_u32(&stage_bar[tid >> 5]);
   uint32_t sphase = 0, spending = 0;
@@ -266,10 +258,26 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
           ids[u] = a.buckets[bstart[t] + (idx - pref[t])];
         }
       }
+      // Dedupe on the CTA's bitmap (one bit a base point): the thread whose atomicOr sets
+      // an id's bit reports it new, so every distinct id is listed exactly once.  Every
+      // atomic of the round is issued before any result is used, so the round costs one
+      // L2 round trip, not kUnroll of them.  (A shared-memory id set in front of the bitmap
+      // measured slower once rows were staged: its 32 KB cost resident CTAs.)
+      uint32_t old[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
-        if (ids[u] >= 0 && dedupe_new(bitmap, ids[u]))
-          list[lbase + atomicAdd(&rcnt[r % 3], 1)] = ids[u];
+      for (int u = 0; u < kUnroll; ++u)
+        old[u] = ids[u] >= 0 ? atomicOr(&bitmap[ids[u] >> 5], 1u << (ids[u] & 31)) : ~0u;
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {  // append the new ids: one shared atomic a warp
+        const bool fresh = !(old[u] & (1u << (ids[u] & 31)));
+        const unsigned m = __ballot_sync(0xffffffffu, fresh);
+        if (m) {
+          const int leader = __ffs(m) - 1;
+          int wbase = 0;
+          if (lane == leader) wbase = atomicAdd(&rcnt[r % 3], __popc(m));
+          wbase = __shfl_sync(0xffffffffu, wbase, leader);
+          if (fresh) list[lbase + wbase + __popc(m & ((1u << lane) - 1u))] = ids[u];
+        }
       }
       __syncthreads();
       const int nl = lbase + rcnt[r % 3];  // uniform: rcnt[r % 3] is not written again before round r+3
