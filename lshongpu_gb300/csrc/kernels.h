@@ -129,7 +129,9 @@ struct LshQueryArgs {
   int vec4;                   // rows are 16-byte aligned float4 runs (d % 4 == 0)
   unsigned long long* stats;  // optional: += bucket entries walked, distinct candidates
   int* err;                   // device error flag (3: a row-copy wait timed out)
-  int stage;                  // set by launch_lsh_query: rows staged by bulk copies
+  int stage;                  // set by lsh_query_plan: rows staged by bulk copies
+  int walk_grid;              // set by lsh_query_plan: CTAs of the bucket-walk kernel (split path)
+  const int* qlist;           // internal: queries to answer ([0] = count, then indices); nullptr = all
 };
 void launch_lsh_query(const LshQueryArgs& a, struct ::lshg_point_s* out, cudaStream_t s);
 

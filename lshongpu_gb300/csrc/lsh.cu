@@ -35,6 +35,8 @@ constexpr int kScoreAt = 1024;                // score the distinct list once it
 constexpr int kListCap = kScoreAt + kRound;   // a round adds at most kRound ids
 constexpr int kStageRows = 16;                // rows a warp stages per bulk-copy batch
 constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268 at 16 rows x 8 warps)
+constexpr int kWalkCtasPerSm = 4;             // bucket-walk CTAs an SM (split path; one bitmap each)
+constexpr int kSplitCap = 8192;               // distinct candidates a query listed by the walk
 constexpr int kQueryCtasPerSm = 2;            // resident query CTAs an SM (register budget; d = 128
                                               // staging, 66 KB a CTA, allows two)
 
@@ -212,7 +214,9 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   }
   __syncthreads();
 
-  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
+  const int nloop = a.qlist ? a.qlist[0] : a.nq;
+  for (int ii = blockIdx.x; ii < nloop; ii += gridDim.x) {
+    const int qi = a.qlist ? a.qlist[1 + ii] : ii;
     for (int j = tid; j < dpad; j += kQThreads) qr[j] = j < a.d ? a.q[(int64_t)qi * a.d + j] : 0.0f;
     if (a.sketched) {
       if (a.sketch_kind == 6) {
@@ -350,6 +354,147 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   if (a.stage && !sok) stage_wait(bar_w, spending, nullptr);  // a timed-out copy may still land
 }
 
+// Split path, step 1 (exact scoring with staged rows): walk each query's buckets, drop
+// repeats on the CTA's bitmap and write the distinct ids to cand[q][0..cap); ccnt[q] =
+// distinct count (a query with more than cap is listed in ovf for the fused kernel, and
+// its walk stops there).  No scoring state, so one barrier a round and little shared
+// memory: many CTAs an SM keep the walk's loads and atomics in flight.
+__global__ void __launch_bounds__(kQThreads) lsh_walk_kernel(LshQueryArgs a, int* __restrict__ cand, int cap,
+                                                             int* __restrict__ ccnt, int* __restrict__ ovf) {
+  __shared__ int bstart[kMaxTables], pref[kMaxTables + 1];
+  __shared__ int wcnt;
+  uint32_t* bitmap = a.bitmaps + (int64_t)blockIdx.x * ((a.n + 31) / 32);
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
+    for (int t = tid; t < a.tables; t += kQThreads) {
+      const int key = a.qkeys[(int64_t)qi * a.tables + t];
+      int st = 0, en = 0;  // a key outside the table addresses no bucket
+      if (key < a.tableSize) {
+        st = a.offsets[(int64_t)t * a.tableSize + key];
+        en = (key >= a.tableSize - 1) ? (int)(t * a.n + a.n) : a.offsets[(int64_t)t * a.tableSize + key + 1];
+      }
+      bstart[t] = st;
+      pref[t + 1] = en - st;
+    }
+    if (tid == 0) wcnt = 0;
+    __syncthreads();
+    if (tid == 0) {
+      pref[0] = 0;
+      for (int t = 0; t < a.tables; ++t) pref[t + 1] += pref[t];
+    }
+    __syncthreads();
+    const int total = pref[a.tables];
+    int* dst = cand + (int64_t)qi * cap;
+    int walked = total;  // entries whose bits may be set (uniform)
+    for (int base = 0; base < total; base += kRound) {
+      // a query past cap goes to the fused kernel anyway: stop walking it (the OR makes the
+      // decision uniform; wcnt only grows, so a stale read only delays it a round)
+      if (base > 0 && __syncthreads_or(wcnt > cap)) {
+        walked = base;
+        break;
+      }
+      int ids[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        const int idx = base + u * kQThreads + tid;
+        ids[u] = -1;
+        if (idx < total) {
+          const int t = entry_table(pref, a.tables, idx);
+          ids[u] = a.buckets[bstart[t] + (idx - pref[t])];
+        }
+      }
+      uint32_t old[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u)
+        old[u] = ids[u] >= 0 ? atomicOr(&bitmap[ids[u] >> 5], 1u << (ids[u] & 31)) : ~0u;
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        const bool fresh = !(old[u] & (1u << (ids[u] & 31)));
+        const unsigned m = __ballot_sync(0xffffffffu, fresh);
+        if (m) {
+          const int leader = __ffs(m) - 1;
+          int wbase = 0;
+          if (lane == leader) wbase = atomicAdd(&wcnt, __popc(m));
+          wbase = __shfl_sync(0xffffffffu, wbase, leader);
+          const int pos = wbase + __popc(m & ((1u << lane) - 1u));
+          if (fresh && pos < cap) dst[pos] = ids[u];
+        }
+      }
+    }
+    __syncthreads();  // every atomic of the query is done: wcnt is final, the bitmap may be cleared
+    const int distinct = wcnt;
+    for (int idx = tid; idx < walked; idx += kQThreads) {
+      const int t = entry_table(pref, a.tables, idx);
+      bitmap[a.buckets[bstart[t] + (idx - pref[t])] >> 5] = 0u;
+    }
+    if (tid == 0) {
+      ccnt[qi] = distinct;
+      if (distinct > cap) ovf[1 + atomicAdd(ovf, 1)] = qi;  // the fused kernel counts it
+      else if (a.stats) {
+        atomicAdd(a.stats, (unsigned long long)total);
+        atomicAdd(a.stats + 1, (unsigned long long)distinct);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Split path, step 2: score each listed query's distinct candidates (rows staged by bulk
+// copies, staged_key) into its top-C and write the first k.  Queries whose lists
+// overflowed are left to the fused kernel.
+template <int DIST>
+__global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm)
+    lsh_score_kernel(LshQueryArgs a, const int* __restrict__ cand, int cap, const int* __restrict__ ccnt,
+                     lshg_point* __restrict__ out) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int NW = kQThreads / 32;
+  const uint32_t stage_slot = stage_slot_bytes(a.d);
+  const uint32_t stage_bytes = (uint32_t)(NW * kStageRows) * stage_slot;
+  uint64_t* kept = reinterpret_cast<uint64_t*>(smem + stage_bytes);
+  uint64_t* buf = kept + a.C;
+  float* qr = reinterpret_cast<float*>(buf + kQBuf);
+  const int dpad = (a.d + 3) & ~3;
+  __shared__ int cnt_s;
+  __shared__ uint64_t thr_s;
+  __shared__ __align__(8) uint64_t stage_bar[NW];
+  TopCShared S{kept, buf, &cnt_s, &thr_s, a.C, kQBuf};
+  const int tid = threadIdx.x;
+  unsigned char* stage_w = smem + (uint32_t)((tid >> 5) * kStageRows) * stage_slot;
+  const uint32_t bar_w = tc::smem_u32(&stage_bar[tid >> 5]);
+  uint32_t sphase = 0, spending = 0;
+  bool sok = true;  // warp-uniform
+  if (tid < NW) tc::mbar_init(tc::smem_u32(&stage_bar[tid]), 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  __syncthreads();
+  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
+    const int c = ccnt[qi];
+    if (c > cap) continue;  // uniform: the fused kernel answers this query
+    for (int j = tid; j < dpad; j += kQThreads) qr[j] = j < a.d ? a.q[(int64_t)qi * a.d + j] : 0.0f;
+    topc_init(S, 1);
+    __syncthreads();
+    const float qn = (DIST == DIST_ANGULAR) ? a.qnorm[qi] : 1.0f;
+    const int* lst = cand + (int64_t)qi * cap;
+    uint64_t thr = kEmptyKey;
+    for (int i0 = 0; i0 < c; i0 += kQThreads) {
+      const int i = i0 + tid;
+      const uint64_t key = staged_key<DIST>(a, i < c ? lst[i] : -1, qr, qn, stage_w, bar_w, sphase, sok, spending);
+      if (i < c) topc_push(S, 0, key, thr);
+      topc_flush<true>(S, 1, thr == kEmptyKey ? a.C - 1 : kQBuf - kQThreads);
+      thr = thr_s;
+    }
+    topc_flush<true>(S, 1, 0);
+    for (int i = tid; i < a.k; i += kQThreads) {
+      const uint64_t kk = i < a.C ? kept[i] : kEmptyKey;
+      lshg_point pt;
+      if (kk == kEmptyKey) { pt.ID = -1; pt.distance = kEmptyDistance; }
+      else { pt.ID = key_id(kk); pt.distance = key_dist(kk); }
+      out[(int64_t)qi * a.k + i] = pt;
+    }
+    __syncthreads();
+  }
+  if (!sok) stage_wait(bar_w, spending, nullptr);  // a timed-out copy may still land
+}
+
 }  // namespace
 
 void launch_lsh_build(const uint16_t* keys, int64_t n, int tables, int tableSize, int* offsets, int* buckets,
@@ -399,6 +544,38 @@ void lsh_query_plan(LshQueryArgs& a, int max_grid) {
     }
   }
   a.grid = std::max(1, std::min(std::min(max_grid, a.nq), num_sms() * std::max(1, per)));
+  a.walk_grid = a.stage ? std::max(1, std::min(a.nq, num_sms() * kWalkCtasPerSm)) : 0;
+}
+
+// Distinct-candidate slots a query on the split path: at most kSplitCap, and no more than
+// 1 GiB of lists for the batch (0 = the batch takes the fused kernel).
+static int split_cap(int nq) {
+  const int64_t by_mem = ((int64_t)1 << 30) / (4 * (int64_t)std::max(nq, 1));
+  const int cap = (int)std::min<int64_t>(kSplitCap, by_mem / 256 * 256);
+  return cap >= 1024 ? cap : 0;
+}
+
+template <int DV>
+static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg_point* out, cudaStream_t s) {
+  DevBuf<int> cand((size_t)a.nq * cap, s), ccnt((size_t)a.nq, s), ovf((size_t)a.nq + 1, s);
+  LSHG_CUDA(cudaMemsetAsync(ovf.ptr, 0, sizeof(int), s));
+  lsh_walk_kernel<<<a.walk_grid, kQThreads, 0, s>>>(a, cand.ptr, cap, ccnt.ptr, ovf.ptr);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+  const size_t ssmem = lsh_stage_bytes(a.d) + (size_t)(a.C + kQBuf) * 8 + (size_t)((a.d + 3) & ~3) * 4 + 16;
+  LSHG_CUDA(cudaFuncSetAttribute(lsh_score_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem));
+  int per = 0;
+  LSHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lsh_score_kernel<DV>, kQThreads, ssmem));
+  const int sgrid = std::max(1, std::min(a.nq, num_sms() * std::max(1, per)));
+  lsh_score_kernel<DV><<<sgrid, kQThreads, ssmem, s>>>(a, cand.ptr, cap, ccnt.ptr, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+  LshQueryArgs f = a;  // queries with more than cap distinct candidates: the fused kernel
+  f.qlist = ovf.ptr;
+  LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem));
+  lsh_query_kernel<DV><<<a.grid, kQThreads, fused_smem, s>>>(f, out);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
 }
 
 void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
@@ -410,6 +587,16 @@ void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
   size_t smem = lsh_query_smem(a);
   LSHG_REQUIRE(smem <= 200 * 1024, "LSH: candidate set too large for shared memory");
   ProfScope _ps("lsh_query", s);
+  const int cap = a.stage ? split_cap(a.nq) : 0;
+  if (cap > 0) {  // exact scoring with staged rows: walk, then score (overflow: fused)
+    switch (a.dist) {
+      case DIST_ANGULAR: launch_split<DIST_ANGULAR>(a, cap, smem, out, s); break;
+      case DIST_JACCARD: launch_split<DIST_JACCARD>(a, cap, smem, out, s); break;
+      case DIST_EUCLID: launch_split<DIST_EUCLID>(a, cap, smem, out, s); break;
+      default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "LSH: invalid distance function");
+    }
+    return;
+  }
 #define LSHG_LQ(DV)                                                                                        \
   do {                                                                                                     \
     LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \

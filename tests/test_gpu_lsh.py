@@ -91,6 +91,32 @@ def test_crosspoly_many_candidates_and_counters(engine, orc, d, P):
     assert idx.query_counters() == (int(ent.sum()), int(dis.sum()))
 
 
+def test_crosspoly_mixed_list_sizes_one_batch(engine, orc):
+    """One batch where 24 queries (in a 30,000-point cluster) have more distinct candidates
+    than the bucket walk lists and go through the fused kernel, and 40 (among 2,000 small
+    clusters) have a few hundred to a few thousand and are scored from their lists; both
+    halves must equal the oracle and the counters the oracle's totals."""
+    d, P, L, bits, n = D, 128, 12, 8, 40000
+    x = np.concatenate([datasets.clustered(30000, d, 71, count=1, center_seed=55),
+                        datasets.clustered(10000, d, 72, count=2000, center_seed=56)])
+    q = np.concatenate([datasets.clustered(24, d, 73, count=1, center_seed=55),
+                        datasets.clustered(40, d, 74, count=2000, center_seed=56)])
+    S = 1 << bits
+    idx = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=bits,
+                       tables=L, options=engine.make_options(cp_hashes=1))
+    xn, qn = orc.normalize(x), orc.normalize(q)
+    diag = engine.random_plus_minus(P * L * 3)
+    oqk = orc.crosspoly(qn, P, L, 1, 3, diag)
+    ooff, obk = orc.lsh_build(orc.crosspoly(xn, P, L, 1, 3, diag), L, S)
+    ent, dis = walked_and_distinct(oqk, ooff, obk, L, S, n)
+    assert (dis > 8192).sum() == 24 and (dis <= 8192).sum() == 40  # the case this test is for
+    res = idx.query(q, 32)
+    ids, ds = orc.lsh_query(xn, qn, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, 1, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
+    assert idx.query_counters() == (int(ent.sum()), int(dis.sum()))
+
+
 def test_simhash_keys_sketched_query(engine, orc):
     n, nq, L, bits, W = 3000, 12, 6, 10, 8
     x, q = data(n, nq, seed=31)
