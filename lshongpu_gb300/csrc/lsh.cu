@@ -478,9 +478,19 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm)
     for (int i0 = 0; i0 < c; i0 += kQThreads) {
       const int i = i0 + tid;
       const uint64_t key = staged_key<DIST>(a, i < c ? lst[i] : -1, qr, qn, stage_w, bar_w, sphase, sok, spending);
-      if (i < c) topc_push(S, 0, key, thr);
-      topc_flush<true>(S, 1, thr == kEmptyKey ? a.C - 1 : kQBuf - kQThreads);
-      thr = thr_s;
+      // until the list is full every key is pushed: fold as soon as it can be filled; later
+      // fold only when the buffer could not take another sub-round (one barrier otherwise)
+      const int limit = thr == kEmptyKey ? a.C - 1 : kQBuf - kQThreads;
+      bool over = false;
+      if (i < c && key < thr) {
+        const int pos = atomicAdd(&cnt_s, 1);
+        buf[pos] = key;
+        over = pos >= limit;
+      }
+      if (__syncthreads_or(over)) {
+        topc_flush<true>(S, 1, limit);
+        thr = thr_s;
+      }
     }
     topc_flush<true>(S, 1, 0);
     for (int i = tid; i < a.k; i += kQThreads) {
