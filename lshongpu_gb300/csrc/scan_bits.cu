@@ -183,7 +183,7 @@ void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, con
                int splits, uint64_t* out, cudaStream_t s) {
   if (C <= 128) launch_cfg<OP, 32, 256, 1, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
   else if (C <= 1024) launch_cfg<OP, 8, 512, 2, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else launch_cfg<OP, 2, 1024, 4, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  else launch_cfg<OP, 2, 2048, 4, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);  // long folds: fewer
 }
 
 // Row width specialised for each sketch type's usual size (1024-bit SimHash = 8 chunks,
