@@ -37,6 +37,7 @@ constexpr int kStageRows = 16;                // rows a warp stages per bulk-cop
 constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268 at 16 rows x 8 warps)
 constexpr int kWalkCtasPerSm = 4;             // bucket-walk CTAs an SM (split path; one bitmap each)
 constexpr int kSplitCap = 8192;               // distinct candidates a query listed by the walk
+constexpr int kScoreCtasPerSm = 3;            // scoring CTAs an SM (register budget: 80 a thread)
 constexpr int kQueryCtasPerSm = 2;            // resident query CTAs an SM (register budget; d = 128
                                               // staging, 66 KB a CTA, allows two)
 
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(kQThreads) lsh_walk_kernel(LshQueryArgs a, int
 // copies, staged_key) into its top-C and write the first k.  Queries whose lists
 // overflowed are left to the fused kernel.
 template <int DIST>
-__global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm)
+__global__ void __launch_bounds__(kQThreads, kScoreCtasPerSm)
     lsh_score_kernel(LshQueryArgs a, const int* __restrict__ cand, int cap, const int* __restrict__ ccnt,
                      lshg_point* __restrict__ out) {
   extern __shared__ __align__(128) unsigned char smem[];
