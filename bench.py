@@ -477,6 +477,19 @@ def main():
     if lsh_counts:
         roofline["lsh_entries_per_query"] = lsh_counts[0] / N_QUERY
         roofline["lsh_distinct_per_query"] = lsh_counts[1] / N_QUERY
+    if bound == "popc" and cnt:
+        # the memory side of a sketch scan: every CTA streams the whole base's sketches for
+        # its block of queries (32 a block for C <= 128, 8 up to 1024, 2 beyond), bytes
+        # actually moved to the SMs (mostly from L2) over the kernel time; the integer
+        # roofline above is the one that bounds these batch sizes
+        cand = {"simhash": CAND}.get(args.path, 4096)
+        qb = 32 if cand <= 128 else (8 if cand <= 1024 else 2)
+        row = {"simhash": 128, "wmh": 256, "wmh1": 32}[args.path]
+        streamed = -(-N_QUERY // qb) * N_BASE * row
+        gbs = streamed / (kms / cnt / 1e3) / 1e9
+        roofline["secondary"] = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                                 "work": f"{streamed / 1e9:.1f} GB of sketches streamed a batch "
+                                         f"({-(-N_QUERY // qb)} query blocks x {N_BASE} x {row} B)"}
 
     extras = {}
     if rank == 0 and not args.no_extras:
