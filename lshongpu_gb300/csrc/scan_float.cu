@@ -202,13 +202,15 @@ __global__ void __launch_bounds__((QB / MQ) * 32) scan_float_kernel(
 // queries 8w .. 8w+7 and lane l points 4l .. 4l+3 of each 128-point tile, so a thread
 // keeps an 8 x 4 micro-tile (32 FMAs per dimension step for three shared loads).  A
 // query's top-C list lives in shared memory; candidates that beat the query's threshold
-// (one warp vote a tile) are appended to its 64-key buffer and merged into the list only
+// (one warp vote a tile) are appended to its 32-key buffer and merged into the list only
 // when the buffer fills -- in a short split nearly every tile brings a candidate, and a
 // merge a tile would cost more than the tile's FMAs.  There is no block-level selection
-// protocol and no barrier besides the tile copy's.
+// protocol and no barrier besides the tile copy's.  Held to 128 registers so that two
+// CTAs share an SM whenever their shared memory fits (d <= ~106 at C = 32).
 // ---------------------------------------------------------------------------------
 constexpr int kRegQB = 64;
-constexpr int kRegBuf = 64;  // candidate keys a query buffers before a merge
+constexpr int kRegBuf = 32;  // candidate keys a query buffers before a merge
+constexpr size_t kRegTwoCtaSmem = 112 * 1024;  // shared memory that lets two CTAs share an SM
 
 __host__ __device__ inline size_t reg_scan_smem(int d, int C, int nbuf) {
   size_t off = 0;
@@ -299,7 +301,7 @@ __device__ __noinline__ uint64_t merge_candidates(uint64_t* list, uint64_t k0, u
 }
 
 template <int DIST, int EC>
-__global__ void __launch_bounds__(256, 1) scan_float_reg_kernel(
+__global__ void __launch_bounds__(256, 2) scan_float_reg_kernel(
     const float* __restrict__ xt, int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
     int nq, const float* __restrict__ qnorm, int tiles_per_split, int splits, int nbuf, uint64_t* __restrict__ out) {
   constexpr int C = 32 * EC;
@@ -478,8 +480,11 @@ template <int DIST>
 bool try_launch_reg(const float* xt, int64_t n, int d, const float* xnorm, const float* q, int nq,
                     const float* qnorm, int C, int splits, uint64_t* out, cudaStream_t s) {
   if (C > 128) return false;
+  // two CTAs an SM (one tile buffer: while one CTA copies, the other computes) when the
+  // shared memory allows, else one CTA with a double-buffered tile
   const size_t cap = 220 * 1024;
-  int nbuf = reg_scan_smem(d, C, 2) <= cap ? 2 : (reg_scan_smem(d, C, 1) <= cap ? 1 : 0);
+  int nbuf = reg_scan_smem(d, C, 1) <= kRegTwoCtaSmem ? 1
+             : (reg_scan_smem(d, C, 2) <= cap ? 2 : (reg_scan_smem(d, C, 1) <= cap ? 1 : 0));
   if (!nbuf) return false;
   if (C == 32) launch_reg<DIST, 1>(xt, n, d, xnorm, q, nq, qnorm, splits, nbuf, out, s);
   else if (C == 64) launch_reg<DIST, 2>(xt, n, d, xnorm, q, nq, qnorm, splits, nbuf, out, s);
@@ -530,8 +535,9 @@ void launch_dist(const float* xt, int64_t n, int d, const float* xnorm, const fl
 }  // namespace
 
 int scan_float_splits(int64_t n, int nq, int C) {
-  // C <= 128 runs the register-blocked kernel (one 64-query CTA an SM), larger C the
-  // general one (two CTAs an SM); pick the split count whose grid fills whole waves best
+  // C <= 128 runs the register-blocked kernel (64-query CTAs; the split count is sized as
+  // for one an SM, a second one an SM, where it fits, hides the first one's tile copies),
+  // larger C the general one (two CTAs an SM); pick the split count whose grid fills whole waves best
   // among those giving at least ~2 CTAs an SM slot, at most 4x that and 64
   const int QB = C <= 128 ? kRegQB : (C <= 1024 ? 8 : 2);
   const int slots = num_sms() * (C <= 128 ? 1 : 2);
