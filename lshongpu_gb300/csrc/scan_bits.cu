@@ -67,8 +67,9 @@ __device__ __forceinline__ int word_score(uint32_t a, uint32_t b) {
 // limit" -- no block barrier in between.
 // NC > 0: rows of exactly NC 128-bit chunks, loops fully unrolled without bounds tests;
 // NC = 0: any row width up to kMaxChunks chunks (runtime bound).
-template <int OP, int QB, int KBUF, int T, int NC>
-__global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __restrict__ xst, int64_t n, int wp, int words,
+// MINB: resident CTAs an SM the register budget is sized for.
+template <int OP, int QB, int KBUF, int T, int NC, int MINB = 2>
+__global__ void __launch_bounds__(256, MINB) scan_bits_kernel(const uint32_t* __restrict__ xst, int64_t n, int wp, int words,
                                                         int sbytes, const uint32_t* __restrict__ qs, int nq, int C,
                                                         int tiles_per_split, int splits, uint64_t* __restrict__ out) {
   static_assert(KBUF >= T * kTile, "append buffer must absorb T tiles");
@@ -163,12 +164,12 @@ __global__ void __launch_bounds__(256, 2) scan_bits_kernel(const uint32_t* __res
   }
 }
 
-template <int OP, int QB, int KBUF, int T, int NC>
+template <int OP, int QB, int KBUF, int T, int NC, int MINB = 2>
 void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                 int splits, uint64_t* out, cudaStream_t s) {
   ProfScope _ps("scan_bits", s);
   size_t smem = bits_layout(wp, QB, C, KBUF).total;
-  auto kern = scan_bits_kernel<OP, QB, KBUF, T, NC>;
+  auto kern = scan_bits_kernel<OP, QB, KBUF, T, NC, MINB>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int ntiles = ceil_div(n, kTile);
   int tps = ceil_div(ntiles, splits);
@@ -182,7 +183,9 @@ template <int OP, int NC>
 void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                int splits, uint64_t* out, cudaStream_t s) {
   if (C <= 128) launch_cfg<OP, 32, 256, 1, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else if (C <= 1024) launch_cfg<OP, 8, 512, 2, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  // up to 1024: 4 queries a block (49 KB at C = 1024) so that three CTAs share an SM and hide
+  // one another's fold barriers; the base is streamed twice as often, which L2 absorbs
+  else if (C <= 1024) launch_cfg<OP, 4, 512, 2, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
   else launch_cfg<OP, 2, 2048, 4, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);  // long folds: fewer
 }
 
@@ -199,11 +202,11 @@ void launch_width(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, 
 }  // namespace
 
 int scan_bits_splits(int64_t n, int nq, int C) {
-  // two CTAs an SM; for C <= 128 pick the split count whose grid fills whole waves best,
+  // two CTAs an SM (three for 128 < C <= 1024); for C <= 128 pick the split count whose grid fills whole waves best,
   // between the count giving ~1.5 CTAs a slot and 4x that (at most 64 splits, >= 4 tiles
   // a split)
-  const int QB = C <= 128 ? 32 : (C <= 1024 ? 8 : 2);
-  const int slots = num_sms() * 2;
+  const int QB = C <= 128 ? 32 : (C <= 1024 ? 4 : 2);
+  const int slots = num_sms() * (C <= 128 || C > 1024 ? 2 : 3);
   const int qblocks = ceil_div(nq, QB);
   const int ntiles = ceil_div(n, kTile);
   const int maxs = std::max(1, std::min(ntiles / 4, 64));
