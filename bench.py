@@ -479,11 +479,11 @@ def main():
         roofline["lsh_distinct_per_query"] = lsh_counts[1] / N_QUERY
     if bound == "popc" and cnt:
         # the memory side of a sketch scan: every CTA streams the whole base's sketches for
-        # its block of queries (32 a block for C <= 128, 4 up to 1024, 2 beyond), bytes
+        # its block of queries (16 a block for C <= 128, 4 up to 1024, 2 beyond), bytes
         # actually moved to the SMs (mostly from L2) over the kernel time; the integer
         # roofline above is the one that bounds these batch sizes
         cand = {"simhash": CAND}.get(args.path, 4096)
-        qb = 32 if cand <= 128 else (4 if cand <= 1024 else 2)
+        qb = 16 if cand <= 128 else (4 if cand <= 1024 else 2)
         row = {"simhash": 128, "wmh": 256, "wmh1": 32}[args.path]
         streamed = -(-N_QUERY // qb) * N_BASE * row
         gbs = streamed / (kms / cnt / 1e3) / 1e9

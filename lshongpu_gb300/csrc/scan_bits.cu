@@ -182,7 +182,7 @@ void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, co
 template <int OP, int NC>
 void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
                int splits, uint64_t* out, cudaStream_t s) {
-  if (C <= 128) launch_cfg<OP, 32, 256, 1, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+  if (C <= 128) launch_cfg<OP, 16, 256, 1, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
   // up to 1024: 4 queries a block (49 KB at C = 1024) so that three CTAs share an SM and hide
   // one another's fold barriers; the base is streamed twice as often, which L2 absorbs
   else if (C <= 1024) launch_cfg<OP, 4, 512, 2, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
@@ -202,11 +202,11 @@ void launch_width(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, 
 }  // namespace
 
 int scan_bits_splits(int64_t n, int nq, int C) {
-  // two CTAs an SM (three for 128 < C <= 1024); for C <= 128 pick the split count whose grid fills whole waves best,
+  // three CTAs an SM (two for C > 1024); for C <= 128 pick the split count whose grid fills whole waves best,
   // between the count giving ~1.5 CTAs a slot and 4x that (at most 64 splits, >= 4 tiles
   // a split)
-  const int QB = C <= 128 ? 32 : (C <= 1024 ? 4 : 2);
-  const int slots = num_sms() * (C <= 128 || C > 1024 ? 2 : 3);
+  const int QB = C <= 128 ? 16 : (C <= 1024 ? 4 : 2);
+  const int slots = num_sms() * (C > 1024 ? 2 : 3);
   const int qblocks = ceil_div(nq, QB);
   const int ntiles = ceil_div(n, kTile);
   const int maxs = std::max(1, std::min(ntiles / 4, 64));
