@@ -132,6 +132,7 @@ struct LshQueryArgs {
   int stage;                  // set by lsh_query_plan: rows staged by bulk copies
   int walk_grid;              // set by lsh_query_plan: CTAs of the bucket-walk kernel (split path)
   const int* qlist;           // internal: queries to answer ([0] = count, then indices); nullptr = all
+  int* lists;                 // internal: the fused kernel's distinct-id lists, [grid][list capacity]
 };
 void launch_lsh_query(const LshQueryArgs& a, struct ::lshg_point_s* out, cudaStream_t s);
 

@@ -38,8 +38,8 @@ constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268
 constexpr int kWalkCtasPerSm = 4;             // bucket-walk CTAs an SM (split path; one bitmap each)
 constexpr int kSplitCap = 8192;               // distinct candidates a query listed by the walk
 constexpr int kScoreCtasPerSm = 3;            // scoring CTAs an SM (register budget: 80 a thread)
-constexpr int kQueryCtasPerSm = 2;            // resident query CTAs an SM (register budget; d = 128
-                                              // staging, 66 KB a CTA, allows two)
+constexpr int kQueryCtasPerSm = 3;            // resident fused-kernel CTAs an SM (register budget;
+                                              // d = 128 staging, 66 KB a CTA, allows three)
 
 __global__ void lsh_hist_kernel(const uint16_t* __restrict__ keys, int64_t n, int tables, int S, int* counts) {
   int64_t total = n * tables;
@@ -192,8 +192,10 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   uint64_t* kept = reinterpret_cast<uint64_t*>(smem + stage_bytes);
   uint64_t* buf = kept + a.C;
   uint64_t* rk = buf + kQBuf;  // re-rank keys [C]
-  int* list = reinterpret_cast<int*>(rk + a.C);
-  float* qr = reinterpret_cast<float*>(list + kListCap);
+  // the distinct-id list lives in global memory (L2): kept out of shared memory it lets
+  // three CTAs share an SM
+  int* list = a.lists + (int64_t)blockIdx.x * kListCap;
+  float* qr = reinterpret_cast<float*>(rk + a.C);
   const int dpad = (a.d + 3) & ~3;
   float* qsf = qr + dpad;
   uint32_t* qsk = reinterpret_cast<uint32_t*>(qsf + (a.sketch_kind == 6 ? a.sdim : 0));
@@ -531,7 +533,7 @@ void launch_lsh_build(const uint16_t* keys, int64_t n, int tables, int tableSize
 static size_t lsh_stage_bytes(int d) { return (size_t)(kQThreads / 32) * kStageRows * stage_slot_bytes(d); }
 
 size_t lsh_query_smem(const LshQueryArgs& a) {
-  return (a.stage ? lsh_stage_bytes(a.d) : 0) + (size_t)(2 * a.C + kQBuf) * 8 + (size_t)kListCap * 4 +
+  return (a.stage ? lsh_stage_bytes(a.d) : 0) + (size_t)(2 * a.C + kQBuf) * 8 +
          (size_t)((a.d + 3) & ~3) * 4 + (size_t)(a.sketch_kind == 6 ? a.sdim : 0) * 4 + (size_t)a.wp * 4 + 16;
 }
 
@@ -583,6 +585,8 @@ static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg
   LSHG_CHECK_LAUNCH();
   LshQueryArgs f = a;  // queries with more than cap distinct candidates: the fused kernel
   f.qlist = ovf.ptr;
+  DevBuf<int> lists((size_t)a.grid * kListCap, s);
+  f.lists = lists.ptr;
   LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem));
   lsh_query_kernel<DV><<<a.grid, kQThreads, fused_smem, s>>>(f, out);
   count_launch();
@@ -608,10 +612,13 @@ void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
     }
     return;
   }
+  DevBuf<int> lists((size_t)a.grid * kListCap, s);
+  LshQueryArgs f = a;
+  f.lists = lists.ptr;
 #define LSHG_LQ(DV)                                                                                        \
   do {                                                                                                     \
     LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-    lsh_query_kernel<DV><<<a.grid, kQThreads, smem, s>>>(a, out);                                          \
+    lsh_query_kernel<DV><<<a.grid, kQThreads, smem, s>>>(f, out);                                          \
   } while (0)
   switch (a.dist) {
     case DIST_ANGULAR: LSHG_LQ(DIST_ANGULAR); break;
