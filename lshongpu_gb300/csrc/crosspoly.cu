@@ -7,9 +7,9 @@
 // when y < 0 and index + P otherwise.  Additions are exact-order identical to the
 // reference, so keys are bit-identical.
 //
-// GB300 form: one warp per point holds the padded vector in registers (P/32 values per
-// lane); in-lane butterflies for small offsets, warp shuffles for the rest, and a
-// shuffle arg-max.  The reference instead keeps two P-float scratch rows per thread in
+// GB300 form: a (point, table) unit's padded vector spread over P/32 lanes, 32 values a
+// lane (a warp works on 32/(P/32) units at once); in-lane butterflies for offsets below
+// 32, shuffles inside the lane group for the rest, and a shuffle arg-max.  The reference instead keeps two P-float scratch rows per thread in
 // global memory (crossPolyTope.cuh:120-124).  `hashes` > 1 concatenates independent
 // rotations into one key (key = h0 * 2P + h1 ...), which the reference does not have.
 #include "common.cuh"
@@ -20,76 +20,108 @@ namespace lshg {
 
 namespace {
 
-template <int E>
+// One (point, table) unit per group of G = P / 32 lanes (P >= 32; a warp holds 32 / G
+// units), or per lane for P < 32.  Lane j of a group holds elements [32j, 32j + 32) (all P
+// for P < 32), so butterfly offsets below 32 pair elements inside a lane and only offsets
+// 32 .. P/2 cross lanes (shuffles within the group).  Units are numbered table-major, so
+// the groups of a warp usually share a table and its diagonals.
+// vec: d % 4 == 0 and 16-byte aligned rows -- a lane's 32 values and 32 diagonal signs
+// are read as eight 16-byte loads each (scalar loads were the kernel's bottleneck: 32
+// lanes x 32 scattered words per instruction).
+template <int W>  // values a lane holds: 32 (P >= 32) or P
 __global__ void __launch_bounds__(256) crosspoly_kernel(const float* __restrict__ x, int64_t n, int d, int P,
                                                         int tables, int hashes, int rounds,
-                                                        const int* __restrict__ diag, uint16_t* __restrict__ keys) {
+                                                        const int* __restrict__ diag, uint16_t* __restrict__ keys,
+                                                        bool vec) {
   const int lane = threadIdx.x & 31;
+  const int G = P >= 32 ? P / 32 : 1;  // lanes a unit
+  const int V = 32 / G;                // units a warp step
+  const int j = lane % G, grp = lane / G;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t p = warp; p < n; p += nwarps) {
-    float xin[E];
+  const int64_t units = n * tables;
+  for (int64_t u0 = warp * V; u0 < units; u0 += nwarps * V) {  // warp-uniform
+    const int64_t u = u0 + grp;
+    const bool live = u < units;
+    const int t = live ? (int)(u / n) : 0;
+    const int64_t p = live ? u - (int64_t)t * n : 0;
+    uint32_t key = 0;
+    for (int h = 0; h < hashes; ++h) {
+      float v[W];
+      if (W == 32 && vec) {
+        const float4* xr = reinterpret_cast<const float4*>(x + p * d + j * W);
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      int i = lane * E + e;
-      xin[e] = (i < d) ? x[p * d + i] : 0.0f;
-    }
-    for (int t = 0; t < tables; ++t) {
-      uint32_t key = 0;
-      for (int h = 0; h < hashes; ++h) {
-        float v[E];
+        for (int c = 0; c < W / 4; ++c) {
+          const float4 f = (live && j * W + 4 * c < d) ? __ldg(xr + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[4 * c] = f.x; v[4 * c + 1] = f.y; v[4 * c + 2] = f.z; v[4 * c + 3] = f.w;
+        }
+      } else {
 #pragma unroll
-        for (int e = 0; e < E; ++e) v[e] = xin[e];
-        for (int r = 0; r < rounds; ++r) {
-          const int* dg = diag + ((((int64_t)t * hashes + h) * rounds + r) * P);
+        for (int e = 0; e < W; ++e) {
+          const int i = j * W + e;
+          v[e] = (live && i < d) ? x[p * d + i] : 0.0f;
+        }
+      }
+      for (int r = 0; r < rounds; ++r) {
+        const int* dg = diag + ((((int64_t)t * hashes + h) * rounds + r) * P) + j * W;
+        if (W == 32) {  // P >= 32: all 32 of the lane's elements are inside P
+          const int4* dg4 = reinterpret_cast<const int4*>(dg);
 #pragma unroll
-          for (int e = 0; e < E; ++e) {
-            int i = lane * E + e;
-            if (i < P) v[e] = __fmul_rn(v[e], (float)dg[i]);
+          for (int c = 0; c < W / 4; ++c) {
+            const int4 g = __ldg(dg4 + c);
+            v[4 * c] = __fmul_rn(v[4 * c], (float)g.x);
+            v[4 * c + 1] = __fmul_rn(v[4 * c + 1], (float)g.y);
+            v[4 * c + 2] = __fmul_rn(v[4 * c + 2], (float)g.z);
+            v[4 * c + 3] = __fmul_rn(v[4 * c + 3], (float)g.w);
           }
-          for (int o = P >> 1; o > 0; o >>= 1) {
-            if (o < E) {
+        } else {
 #pragma unroll
-              for (int e = 0; e < E; ++e) {
-                if ((e & o) == 0) {
-                  float a = v[e], b = v[e | o];
-                  v[e] = __fadd_rn(a, b);
-                  v[e | o] = __fsub_rn(a, b);  // upper index: partner - self
-                }
-              }
-            } else {
-              int lo = o / E;
-              bool lower = (lane & lo) == 0;
+          for (int e = 0; e < W; ++e)
+            if (j * W + e < P) v[e] = __fmul_rn(v[e], (float)dg[e]);
+        }
+        // offsets P/2 .. W cross lanes (shuffles inside the group), then W/2 .. 1 pair
+        // elements inside a lane (compile-time offsets keep v in registers)
+        for (int o = P >> 1; o >= W; o >>= 1) {
+          const int lo = o / W;  // partner lane within the group
+          const bool lower = (j & lo) == 0;
 #pragma unroll
-              for (int e = 0; e < E; ++e) {
-                float other = __shfl_xor_sync(0xffffffffu, v[e], lo);
-                v[e] = lower ? __fadd_rn(v[e], other) : __fsub_rn(other, v[e]);
-              }
+          for (int e = 0; e < W; ++e) {
+            const float other = __shfl_xor_sync(0xffffffffu, v[e], lo);
+            v[e] = lower ? __fadd_rn(v[e], other) : __fsub_rn(other, v[e]);
+          }
+        }
+#pragma unroll
+        for (int o = W >> 1; o > 0; o >>= 1) {
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            if ((e & o) == 0) {
+              const float a = v[e], b = v[e | o];
+              v[e] = __fadd_rn(a, b);
+              v[e | o] = __fsub_rn(a, b);  // upper index: partner - self
             }
           }
         }
-        // first maximum of |v| in dimension order
-        float best = -1.0f;
-        int bi = 0x7fffffff;
-        bool bneg = false;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-          int i = lane * E + e;
-          float a = fabsf(v[e]);
-          if (i < P && a > best) { best = a; bi = i; bneg = v[e] < 0.0f; }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          float ob = __shfl_xor_sync(0xffffffffu, best, off);
-          int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-          bool on = __shfl_xor_sync(0xffffffffu, (int)bneg, off) != 0;
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bneg = on; }
-        }
-        uint32_t code = (bi == 0x7fffffff) ? 0u : (bneg ? (uint32_t)bi : (uint32_t)(bi + P));
-        key = key * (uint32_t)(2 * P) + code;
       }
-      if (lane == 0) keys[p * tables + t] = (uint16_t)key;
+      // first maximum of |v| in dimension order
+      float best = -1.0f;
+      int bi = 0x7fffffff;
+      bool bneg = false;
+#pragma unroll
+      for (int e = 0; e < W; ++e) {
+        const int i = j * W + e;
+        const float a = fabsf(v[e]);
+        if (i < P && a > best) { best = a; bi = i; bneg = v[e] < 0.0f; }
+      }
+      for (int off = G >> 1; off > 0; off >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        const bool on = __shfl_xor_sync(0xffffffffu, (int)bneg, off) != 0;
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; bneg = on; }
+      }
+      const uint32_t code = (bi == 0x7fffffff) ? 0u : (bneg ? (uint32_t)bi : (uint32_t)(bi + P));
+      key = key * (uint32_t)(2 * P) + code;
     }
+    if (live && j == 0) keys[p * tables + t] = (uint16_t)key;
   }
 }
 
@@ -99,12 +131,15 @@ void launch_crosspoly(const float* x, int64_t n, int d, int P, int tables, int h
                       const int* diag, uint16_t* keys, cudaStream_t s) {
   if (n <= 0) return;
   LSHG_REQUIRE(P >= d && (P & (P - 1)) == 0 && P <= 1024, "cross-polytope: P must be a power of two >= d, <= 1024");
-  int E = P >= 32 ? P / 32 : 1;
-  int64_t warps = n;
-  int blocks = (int)std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms() * 16);
-  switch (E) {
-#define LSHG_CP(EV) \
-  case EV: crosspoly_kernel<EV><<<blocks, 256, 0, s>>>(x, n, d, P, tables, hashes, rounds, diag, keys); break;
+  const int W = P >= 32 ? 32 : P;                  // values a lane holds
+  const bool vec = d % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(diag) & 15) == 0;
+  const int V = P >= 32 ? 32 / (P / 32) : 32;     // units a warp step
+  const int64_t warps = (n * tables + V - 1) / V;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms() * 16));
+  switch (W) {
+#define LSHG_CP(WV) \
+  case WV: crosspoly_kernel<WV><<<blocks, 256, 0, s>>>(x, n, d, P, tables, hashes, rounds, diag, keys, vec); break;
     LSHG_CP(1) LSHG_CP(2) LSHG_CP(4) LSHG_CP(8) LSHG_CP(16) LSHG_CP(32)
 #undef LSHG_CP
     default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "cross-polytope: unsupported P");
