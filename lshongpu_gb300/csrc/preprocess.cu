@@ -16,7 +16,7 @@ namespace lshg {
 
 namespace {
 
-constexpr int kRowsPerBlock = 64;
+constexpr int kRowsPerBlock = 32;  // small blocks: a 10k-row query batch spreads over every SM
 
 // Stage kRowsPerBlock rows into shared memory with an odd row pitch (conflict-free
 // column walks), then let thread t own row t.
@@ -32,19 +32,21 @@ __global__ void row_norm_kernel(float* __restrict__ x, int64_t n, int d, float* 
     sm[r * pitch + c] = src[i];
   }
   __syncthreads();
+  __shared__ float mags[kRowsPerBlock];
   if (threadIdx.x < rows) {
     const float* row = sm + threadIdx.x * pitch;
     float m = 0.0f;
     for (int j = 0; j < d; ++j) m = __fmaf_rn(row[j], row[j], m);
     m = __fsqrt_rn(m);
-    if (kNormalize) {
-      float* rw = sm + threadIdx.x * pitch;
-      for (int j = 0; j < d; ++j) rw[j] = __fdiv_rn(rw[j], m);
-    } else {
-      norms[row0 + threadIdx.x] = m;
-    }
+    if (kNormalize) mags[threadIdx.x] = m;
+    else norms[row0 + threadIdx.x] = m;
   }
-  if (kNormalize) {
+  if (kNormalize) {  // the divides are independent: every thread takes a share
+    __syncthreads();
+    for (int i = threadIdx.x; i < rows * d; i += blockDim.x) {
+      const int r = i / d, c = i - r * d;
+      sm[r * pitch + c] = __fdiv_rn(sm[r * pitch + c], mags[r]);
+    }
     __syncthreads();
     float* dst = x + row0 * d;
     for (int i = threadIdx.x; i < rows * d; i += blockDim.x) {
