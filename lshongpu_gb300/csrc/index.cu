@@ -501,9 +501,11 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     a.k = k;
     a.vec4 = (I.d % 4 == 0 && (reinterpret_cast<uintptr_t>(I.x.ptr) & 15) == 0) ? 1 : 0;
     lsh_query_plan(a, I.lsh_grid);  // staging choice and grid (resident CTAs)
-    // per-call dedupe bitmaps: concurrent queries on one index never share them
-    DevBuf<uint32_t> bm((size_t)std::max(a.grid, a.walk_grid) * ((I.n + 31) / 32), s);
-    LSHG_CUDA(cudaMemsetAsync(bm.ptr, 0, bm.bytes(), s));
+    // per-call dedupe bitmaps of the fused kernel: concurrent queries on one index never
+    // share them (on the split path the fused kernel only answers overflowing queries and
+    // zeroes a bitmap itself when it gets one)
+    DevBuf<uint32_t> bm((size_t)a.grid * ((I.n + 31) / 32), s);
+    if (a.split_cap == 0) LSHG_CUDA(cudaMemsetAsync(bm.ptr, 0, bm.bytes(), s));
     a.bitmaps = bm.ptr;
     a.stats = I.qstats.ptr;
     a.err = I.qerr.ptr;

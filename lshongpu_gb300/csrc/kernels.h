@@ -124,13 +124,16 @@ struct LshQueryArgs {
   int sdim;
   int C;  // candidate count kept before re-rank (sketched) or pow2 >= k (exact)
   int k;
-  uint32_t* bitmaps;  // per-CTA dedupe bitmaps [grid][ceil(n/32)], zero on entry and exit
+  uint32_t* bitmaps;  // per-CTA dedupe bitmaps of the fused kernel [grid][ceil(n/32)]: zero on
+                      // entry and exit unless bitmap_dirty (the split path never zeroes them)
   int grid;
   int vec4;                   // rows are 16-byte aligned float4 runs (d % 4 == 0)
   unsigned long long* stats;  // optional: += bucket entries walked, distinct candidates
   int* err;                   // device error flag (3: a row-copy wait timed out)
   int stage;                  // set by lsh_query_plan: rows staged by bulk copies
   int walk_grid;              // set by lsh_query_plan: CTAs of the bucket-walk kernel (split path)
+  int split_cap;              // set by lsh_query_plan: distinct ids a query the walk lists (0: fused path)
+  int bitmap_dirty;           // internal: the fused kernel zeroes its bitmap before its first query
   const int* qlist;           // internal: queries to answer ([0] = count, then indices); nullptr = all
   int* lists;                 // internal: the fused kernel's distinct-id lists, [grid][list capacity]
 };

@@ -35,8 +35,11 @@ constexpr int kScoreAt = 1024;                // score the distinct list once it
 constexpr int kListCap = kScoreAt + kRound;   // a round adds at most kRound ids
 constexpr int kStageRows = 16;                // rows a warp stages per bulk-copy batch
 constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268 at 16 rows x 8 warps)
-constexpr int kWalkCtasPerSm = 4;             // bucket-walk CTAs an SM (split path; one bitmap each)
+constexpr int kWalkCtasPerSm = 3;             // bucket-walk CTAs an SM (split path; 64 KB id set each)
+constexpr int kWalkSlotBits = 14;
+constexpr int kWalkSlots = 1 << kWalkSlotBits;  // slots of a walk CTA's shared id set
 constexpr int kSplitCap = 8192;               // distinct candidates a query listed by the walk
+static_assert(kSplitCap + kRound <= kWalkSlots * 5 / 8, "walk id set: load factor at most 5/8");
 constexpr int kScoreCtasPerSm = 3;            // scoring CTAs an SM (register budget: 80 a thread)
 constexpr int kQueryCtasPerSm = 3;            // resident fused-kernel CTAs an SM (register budget;
                                               // d = 128 staging, 66 KB a CTA, allows three)
@@ -218,6 +221,10 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   __syncthreads();
 
   const int nloop = a.qlist ? a.qlist[0] : a.nq;
+  if (a.bitmap_dirty && (int)blockIdx.x < nloop) {  // nobody zeroed the bitmap: do it once
+    for (int w = tid; w < (a.n + 31) / 32; w += kQThreads) bitmap[w] = 0u;
+    __syncthreads();
+  }
   for (int ii = blockIdx.x; ii < nloop; ii += gridDim.x) {
     const int qi = a.qlist ? a.qlist[1 + ii] : ii;
     for (int j = tid; j < dpad; j += kQThreads) qr[j] = j < a.d ? a.q[(int64_t)qi * a.d + j] : 0.0f;
@@ -357,45 +364,81 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   if (a.stage && !sok) stage_wait(bar_w, spending, nullptr);  // a timed-out copy may still land
 }
 
-// Split path, step 1 (exact scoring with staged rows): walk each query's buckets, drop
-// repeats on the CTA's bitmap and write the distinct ids to cand[q][0..cap); ccnt[q] =
-// distinct count (a query with more than cap is listed in ovf for the fused kernel, and
-// its walk stops there).  No scoring state, so one barrier a round and little shared
-// memory: many CTAs an SM keep the walk's loads and atomics in flight.
-__global__ void __launch_bounds__(kQThreads) lsh_walk_kernel(LshQueryArgs a, int* __restrict__ cand, int cap,
-                                                             int* __restrict__ ccnt, int* __restrict__ ovf) {
-  __shared__ int bstart[kMaxTables], pref[kMaxTables + 1];
-  __shared__ int wcnt;
-  uint32_t* bitmap = a.bitmaps + (int64_t)blockIdx.x * ((a.n + 31) / 32);
-  const int tid = threadIdx.x, lane = tid & 31;
-  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
-    for (int t = tid; t < a.tables; t += kQThreads) {
+// Bucket bounds of query qi into bstart[t] (first entry of table t's bucket) and pref
+// (pref[0] = 0, pref[t + 1] = entries of tables 0..t), by one warp: 32 tables a pass,
+// prefix sums by shuffles.
+__device__ __forceinline__ void bucket_bounds_warp(const LshQueryArgs& a, int qi, int* bstart, int* pref,
+                                                   int lane) {
+  int carry = 0;
+  for (int t0 = 0; t0 < a.tables; t0 += 32) {
+    const int t = t0 + lane;
+    int st = 0, len = 0;  // a key outside the table addresses no bucket
+    if (t < a.tables) {
       const int key = a.qkeys[(int64_t)qi * a.tables + t];
-      int st = 0, en = 0;  // a key outside the table addresses no bucket
       if (key < a.tableSize) {
         st = a.offsets[(int64_t)t * a.tableSize + key];
-        en = (key >= a.tableSize - 1) ? (int)(t * a.n + a.n) : a.offsets[(int64_t)t * a.tableSize + key + 1];
+        const int en = (key >= a.tableSize - 1) ? (int)(t * a.n + a.n)
+                                                : a.offsets[(int64_t)t * a.tableSize + key + 1];
+        len = en - st;
       }
+    }
+    int v = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (t < a.tables) {
       bstart[t] = st;
-      pref[t + 1] = en - st;
+      pref[t + 1] = carry + v;
     }
+    carry += __shfl_sync(0xffffffffu, v, 31);
+  }
+  if (lane == 0) pref[0] = 0;
+}
+
+// Open-addressing set of point ids in shared memory (kWalkSlots slots, -1 = empty, linear
+// probing from a Fibonacci hash).  True when id was absent.  The walk inserts at most
+// cap + kRound ids a query, well below kWalkSlots, so a free slot is always found; the
+// probe count is bounded all the same.
+__device__ __forceinline__ bool seen_insert(int* seen, int id) {
+  uint32_t h = ((uint32_t)id * 2654435769u) >> (32 - kWalkSlotBits);
+  for (int p = 0; p < kWalkSlots; ++p) {
+    const int prev = atomicCAS(&seen[h], -1, id);
+    if (prev == -1) return true;
+    if (prev == id) return false;
+    h = (h + 1) & (kWalkSlots - 1);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void seen_clear(int* seen, int tid) {
+  for (int i = tid; i < kWalkSlots / 4; i += kQThreads) reinterpret_cast<int4*>(seen)[i] = make_int4(-1, -1, -1, -1);
+}
+
+// Split path, step 1 (exact scoring with staged rows): walk each query's buckets, drop
+// repeats in the CTA's shared-memory id set and write the distinct ids to
+// cand[q][0..cap); ccnt[q] = distinct count (a query with more than cap is listed in ovf
+// for the fused kernel, and its walk stops there).  No scoring state and no global
+// atomics: one barrier a round, and the set is cleared with 16-byte shared stores.
+__global__ void __launch_bounds__(kQThreads, kWalkCtasPerSm)
+    lsh_walk_kernel(LshQueryArgs a, int* __restrict__ cand, int cap, int* __restrict__ ccnt, int* __restrict__ ovf) {
+  extern __shared__ __align__(16) int seen[];  // kWalkSlots ids
+  __shared__ int bstart[kMaxTables], pref[kMaxTables + 1];
+  __shared__ int wcnt;
+  const int tid = threadIdx.x, lane = tid & 31;
+  seen_clear(seen, tid);
+  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
+    // the previous query's last reads of bstart/pref/wcnt precede its closing barrier
+    if (tid < 32) bucket_bounds_warp(a, qi, bstart, pref, lane);
     if (tid == 0) wcnt = 0;
-    __syncthreads();
-    if (tid == 0) {
-      pref[0] = 0;
-      for (int t = 0; t < a.tables; ++t) pref[t + 1] += pref[t];
-    }
     __syncthreads();
     const int total = pref[a.tables];
     int* dst = cand + (int64_t)qi * cap;
-    int walked = total;  // entries whose bits may be set (uniform)
     for (int base = 0; base < total; base += kRound) {
       // a query past cap goes to the fused kernel anyway: stop walking it (the OR makes the
       // decision uniform; wcnt only grows, so a stale read only delays it a round)
-      if (base > 0 && __syncthreads_or(wcnt > cap)) {
-        walked = base;
-        break;
-      }
+      if (base > 0 && __syncthreads_or(wcnt > cap)) break;
       int ids[kUnroll];
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
@@ -406,13 +449,9 @@ __global__ void __launch_bounds__(kQThreads) lsh_walk_kernel(LshQueryArgs a, int
           ids[u] = a.buckets[bstart[t] + (idx - pref[t])];
         }
       }
-      uint32_t old[kUnroll];
-#pragma unroll
-      for (int u = 0; u < kUnroll; ++u)
-        old[u] = ids[u] >= 0 ? atomicOr(&bitmap[ids[u] >> 5], 1u << (ids[u] & 31)) : ~0u;
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
-        const bool fresh = !(old[u] & (1u << (ids[u] & 31)));
+        const bool fresh = ids[u] >= 0 && seen_insert(seen, ids[u]);
         const unsigned m = __ballot_sync(0xffffffffu, fresh);
         if (m) {
           const int leader = __ffs(m) - 1;
@@ -424,13 +463,10 @@ __global__ void __launch_bounds__(kQThreads) lsh_walk_kernel(LshQueryArgs a, int
         }
       }
     }
-    __syncthreads();  // every atomic of the query is done: wcnt is final, the bitmap may be cleared
-    const int distinct = wcnt;
-    for (int idx = tid; idx < walked; idx += kQThreads) {
-      const int t = entry_table(pref, a.tables, idx);
-      bitmap[a.buckets[bstart[t] + (idx - pref[t])] >> 5] = 0u;
-    }
+    __syncthreads();  // every insert of the query is done: wcnt is final, the set may be cleared
+    seen_clear(seen, tid);
     if (tid == 0) {
+      const int distinct = wcnt;
       ccnt[qi] = distinct;
       if (distinct > cap) ovf[1 + atomicAdd(ovf, 1)] = qi;  // the fused kernel counts it
       else if (a.stats) {
@@ -438,7 +474,6 @@ __global__ void __launch_bounds__(kQThreads) lsh_walk_kernel(LshQueryArgs a, int
         atomicAdd(a.stats + 1, (unsigned long long)distinct);
       }
     }
-    __syncthreads();
   }
 }
 
@@ -545,6 +580,14 @@ static int lsh_ctas_per_sm(size_t smem) {
   return per;
 }
 
+// Distinct-candidate slots a query on the split path: at most kSplitCap, and no more than
+// 1 GiB of lists for the batch (0 = the batch takes the fused kernel).
+static int split_cap(int nq) {
+  const int64_t by_mem = ((int64_t)1 << 30) / (4 * (int64_t)std::max(nq, 1));
+  const int cap = (int)std::min<int64_t>(kSplitCap, by_mem / 256 * 256);
+  return cap >= 1024 ? cap : 0;
+}
+
 void lsh_query_plan(LshQueryArgs& a, int max_grid) {
   a.stage = (a.vec4 && !a.sketched && lsh_stage_bytes(a.d) <= (size_t)kStageMaxBytes) ? 1 : 0;
   const size_t smem = lsh_query_smem(a);
@@ -557,22 +600,22 @@ void lsh_query_plan(LshQueryArgs& a, int max_grid) {
     }
   }
   a.grid = std::max(1, std::min(std::min(max_grid, a.nq), num_sms() * std::max(1, per)));
-  a.walk_grid = a.stage ? std::max(1, std::min(a.nq, num_sms() * kWalkCtasPerSm)) : 0;
-}
-
-// Distinct-candidate slots a query on the split path: at most kSplitCap, and no more than
-// 1 GiB of lists for the batch (0 = the batch takes the fused kernel).
-static int split_cap(int nq) {
-  const int64_t by_mem = ((int64_t)1 << 30) / (4 * (int64_t)std::max(nq, 1));
-  const int cap = (int)std::min<int64_t>(kSplitCap, by_mem / 256 * 256);
-  return cap >= 1024 ? cap : 0;
+  a.split_cap = a.stage ? split_cap(a.nq) : 0;
+  a.walk_grid = 0;
+  if (a.split_cap > 0) {
+    constexpr int wsmem = kWalkSlots * 4;
+    LSHG_CUDA(cudaFuncSetAttribute(lsh_walk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, wsmem));
+    int wper = 0;
+    LSHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wper, lsh_walk_kernel, kQThreads, wsmem));
+    a.walk_grid = std::max(1, std::min(a.nq, num_sms() * std::max(1, wper)));
+  }
 }
 
 template <int DV>
 static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg_point* out, cudaStream_t s) {
   DevBuf<int> cand((size_t)a.nq * cap, s), ccnt((size_t)a.nq, s), ovf((size_t)a.nq + 1, s);
   LSHG_CUDA(cudaMemsetAsync(ovf.ptr, 0, sizeof(int), s));
-  lsh_walk_kernel<<<a.walk_grid, kQThreads, 0, s>>>(a, cand.ptr, cap, ccnt.ptr, ovf.ptr);
+  lsh_walk_kernel<<<a.walk_grid, kQThreads, kWalkSlots * 4, s>>>(a, cand.ptr, cap, ccnt.ptr, ovf.ptr);
   count_launch();
   LSHG_CHECK_LAUNCH();
   const size_t ssmem = lsh_stage_bytes(a.d) + (size_t)(a.C + kQBuf) * 8 + (size_t)((a.d + 3) & ~3) * 4 + 16;
@@ -585,6 +628,7 @@ static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg
   LSHG_CHECK_LAUNCH();
   LshQueryArgs f = a;  // queries with more than cap distinct candidates: the fused kernel
   f.qlist = ovf.ptr;
+  f.bitmap_dirty = 1;
   DevBuf<int> lists((size_t)a.grid * kListCap, s);
   f.lists = lists.ptr;
   LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem));
@@ -602,7 +646,7 @@ void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
   size_t smem = lsh_query_smem(a);
   LSHG_REQUIRE(smem <= 200 * 1024, "LSH: candidate set too large for shared memory");
   ProfScope _ps("lsh_query", s);
-  const int cap = a.stage ? split_cap(a.nq) : 0;
+  const int cap = a.split_cap;
   if (cap > 0) {  // exact scoring with staged rows: walk, then score (overflow: fused)
     switch (a.dist) {
       case DIST_ANGULAR: launch_split<DIST_ANGULAR>(a, cap, smem, out, s); break;
