@@ -8,8 +8,10 @@
 // reference, so keys are bit-identical.
 //
 // GB300 form: a (point, table) unit's padded vector spread over P/32 lanes, 32 values a
-// lane (a warp works on 32/(P/32) units at once); in-lane butterflies for offsets below
-// 32, shuffles inside the lane group for the rest, and a shuffle arg-max.  The reference instead keeps two P-float scratch rows per thread in
+// lane in 4-float chunks dealt round-robin (a warp works on 32/(P/32) units at once, and
+// a group's 16-byte loads read contiguous runs); butterflies of the chunk bits and of the
+// two lowest bits run inside a lane, those of the lane bits are shuffles, and the arg-max
+// ends in shuffles.  The reference instead keeps two P-float scratch rows per thread in
 // global memory (crossPolyTope.cuh:120-124).  `hashes` > 1 concatenates independent
 // rotations into one key (key = h0 * 2P + h1 ...), which the reference does not have.
 #include "common.cuh"
@@ -20,19 +22,28 @@ namespace lshg {
 
 namespace {
 
+// v * g for a diagonal entry g = +1 or -1: the product is exact, so it is v with its sign
+// bit flipped when g < 0 (no int-to-float conversion and no multiply)
+__device__ __forceinline__ float times_sign(float v, int g) {
+  return __int_as_float(__float_as_int(v) ^ (g & (int)0x80000000u));
+}
+
 // One (point, table) unit per group of G = P / 32 lanes (P >= 32; a warp holds 32 / G
-// units), or per lane for P < 32.  Lane j of a group holds elements [32j, 32j + 32) (all P
-// for P < 32), so butterfly offsets below 32 pair elements inside a lane and only offsets
-// 32 .. P/2 cross lanes (shuffles within the group).  Units are numbered table-major, so
-// the groups of a warp usually share a table and its diagonals.
-// vec: d % 4 == 0 and 16-byte aligned rows -- a lane's 32 values and 32 diagonal signs
-// are read as eight 16-byte loads each (scalar loads were the kernel's bottleneck: 32
-// lanes x 32 scattered words per instruction).
+// units), or per lane for P < 32.  The padded vector is cut into 4-float chunks dealt
+// round-robin over the group: lane j holds chunks j, j + G, j + 2G, ..., so register
+// e = 4c + r of lane j is element i = 4(Gc + j) + r.  A group's 16-byte loads then read
+// contiguous runs of the row and of the diagonal.  Butterfly offsets 1 and 2 (bits of r)
+// and offsets 4G and up (bits of c) pair registers inside a lane; offsets 4 .. 2G (bits of
+// j) pair lanes of the group (shuffles).  Units are numbered table-major, so the groups of
+// a warp usually share a table and its diagonals.
+// vec: d % 4 == 0 and 16-byte aligned rows -- chunks are read as 16-byte loads.
 template <int W>  // values a lane holds: 32 (P >= 32) or P
 __global__ void __launch_bounds__(256) crosspoly_kernel(const float* __restrict__ x, int64_t n, int d, int P,
                                                         int tables, int hashes, int rounds,
                                                         const int* __restrict__ diag, uint16_t* __restrict__ keys,
                                                         bool vec) {
+  constexpr int R = W < 4 ? W : 4;  // values a chunk
+  constexpr int NC = W / R;         // chunks a lane
   const int lane = threadIdx.x & 31;
   const int G = P >= 32 ? P / 32 : 1;  // lanes a unit
   const int V = 32 / G;                // units a warp step
@@ -49,66 +60,80 @@ __global__ void __launch_bounds__(256) crosspoly_kernel(const float* __restrict_
     for (int h = 0; h < hashes; ++h) {
       float v[W];
       if (W == 32 && vec) {
-        const float4* xr = reinterpret_cast<const float4*>(x + p * d + j * W);
+        const float4* xr = reinterpret_cast<const float4*>(x + p * d);
 #pragma unroll
-        for (int c = 0; c < W / 4; ++c) {
-          const float4 f = (live && j * W + 4 * c < d) ? __ldg(xr + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int c = 0; c < NC; ++c) {
+          const int ch = G * c + j;
+          const float4 f = (live && 4 * ch < d) ? __ldg(xr + ch) : make_float4(0.f, 0.f, 0.f, 0.f);
           v[4 * c] = f.x; v[4 * c + 1] = f.y; v[4 * c + 2] = f.z; v[4 * c + 3] = f.w;
         }
       } else {
 #pragma unroll
         for (int e = 0; e < W; ++e) {
-          const int i = j * W + e;
+          const int i = R * (G * (e / R) + j) + e % R;
           v[e] = (live && i < d) ? x[p * d + i] : 0.0f;
         }
       }
       for (int r = 0; r < rounds; ++r) {
-        const int* dg = diag + ((((int64_t)t * hashes + h) * rounds + r) * P) + j * W;
+        const int* dg = diag + ((((int64_t)t * hashes + h) * rounds + r) * P);
         if (W == 32) {  // P >= 32: all 32 of the lane's elements are inside P
           const int4* dg4 = reinterpret_cast<const int4*>(dg);
 #pragma unroll
-          for (int c = 0; c < W / 4; ++c) {
-            const int4 g = __ldg(dg4 + c);
-            v[4 * c] = __fmul_rn(v[4 * c], (float)g.x);
-            v[4 * c + 1] = __fmul_rn(v[4 * c + 1], (float)g.y);
-            v[4 * c + 2] = __fmul_rn(v[4 * c + 2], (float)g.z);
-            v[4 * c + 3] = __fmul_rn(v[4 * c + 3], (float)g.w);
+          for (int c = 0; c < NC; ++c) {
+            const int4 g = __ldg(dg4 + G * c + j);
+            v[4 * c] = times_sign(v[4 * c], g.x);
+            v[4 * c + 1] = times_sign(v[4 * c + 1], g.y);
+            v[4 * c + 2] = times_sign(v[4 * c + 2], g.z);
+            v[4 * c + 3] = times_sign(v[4 * c + 3], g.w);
           }
-        } else {
+        } else {  // P < 32: G = 1, register e is element e
 #pragma unroll
-          for (int e = 0; e < W; ++e)
-            if (j * W + e < P) v[e] = __fmul_rn(v[e], (float)dg[e]);
+          for (int e = 0; e < W; ++e) v[e] = times_sign(v[e], dg[e]);
         }
-        // offsets P/2 .. W cross lanes (shuffles inside the group), then W/2 .. 1 pair
-        // elements inside a lane (compile-time offsets keep v in registers)
-        for (int o = P >> 1; o >= W; o >>= 1) {
-          const int lo = o / W;  // partner lane within the group
-          const bool lower = (j & lo) == 0;
+        // offsets P/2 .. 4G: chunk bits, pairs of registers R*o/(4G) apart in a lane
+#pragma unroll
+        for (int oc = NC >> 1; oc > 0; oc >>= 1) {
+#pragma unroll
+          for (int e = 0; e < W; ++e) {
+            if ((e & (R * oc)) == 0) {
+              const float a = v[e], b = v[e | (R * oc)];
+              v[e] = __fadd_rn(a, b);
+              v[e | (R * oc)] = __fsub_rn(a, b);  // upper index: lower - upper
+            }
+          }
+        }
+        // offsets 2G .. 4: lane bits, partner lane j ^ o/4 of the group.  The lower lane
+        // keeps other + v and the upper one other - v = other + (-v): IEEE addition
+        // commutes and subtraction is addition of the negation, so both are one rounded
+        // add of the same operands as the reference's a + b and a - b.
+        for (int lo = G >> 1; lo > 0; lo >>= 1) {
+          const int flip = (j & lo) ? -1 : 1;
 #pragma unroll
           for (int e = 0; e < W; ++e) {
             const float other = __shfl_xor_sync(0xffffffffu, v[e], lo);
-            v[e] = lower ? __fadd_rn(v[e], other) : __fsub_rn(other, v[e]);
+            v[e] = __fadd_rn(other, times_sign(v[e], flip));
           }
         }
+        // offsets 2, 1: bits of r, inside a chunk
 #pragma unroll
-        for (int o = W >> 1; o > 0; o >>= 1) {
+        for (int o = R >> 1; o > 0; o >>= 1) {
 #pragma unroll
           for (int e = 0; e < W; ++e) {
             if ((e & o) == 0) {
               const float a = v[e], b = v[e | o];
               v[e] = __fadd_rn(a, b);
-              v[e | o] = __fsub_rn(a, b);  // upper index: partner - self
+              v[e | o] = __fsub_rn(a, b);
             }
           }
         }
       }
-      // first maximum of |v| in dimension order
+      // first maximum of |v| in dimension order (a lane's element index grows with e)
       float best = -1.0f;
       int bi = 0x7fffffff;
       bool bneg = false;
 #pragma unroll
       for (int e = 0; e < W; ++e) {
-        const int i = j * W + e;
+        const int i = R * (G * (e / R) + j) + e % R;
         const float a = fabsf(v[e]);
         if (i < P && a > best) { best = a; bi = i; bneg = v[e] < 0.0f; }
       }

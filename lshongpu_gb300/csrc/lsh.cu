@@ -439,14 +439,25 @@ __global__ void __launch_bounds__(kQThreads, kWalkCtasPerSm)
       // a query past cap goes to the fused kernel anyway: stop walking it (the OR makes the
       // decision uniform; wcnt only grows, so a stale read only delays it a round)
       if (base > 0 && __syncthreads_or(wcnt > cap)) break;
+      // a warp takes kUnroll * 32 consecutive entries, a lane every 32nd: its table index
+      // only moves forward, so one search a round and a bucket-end compare an entry
       int ids[kUnroll];
+      {
+        const int i0 = base + (tid >> 5) * (kUnroll * 32) + lane;
+        int t = i0 < total ? entry_table(pref, a.tables, i0) : 0;
+        int tend = pref[t + 1], off = bstart[t] - pref[t];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
-        const int idx = base + u * kQThreads + tid;
-        ids[u] = -1;
-        if (idx < total) {
-          const int t = entry_table(pref, a.tables, idx);
-          ids[u] = a.buckets[bstart[t] + (idx - pref[t])];
+        for (int u = 0; u < kUnroll; ++u) {
+          const int idx = i0 + u * 32;
+          ids[u] = -1;
+          if (idx < total) {
+            while (idx >= tend) {  // ends: idx < total = pref[tables]
+              ++t;
+              tend = pref[t + 1];
+              off = bstart[t] - pref[t];
+            }
+            ids[u] = a.buckets[off + idx];
+          }
         }
       }
 #pragma unroll

@@ -200,6 +200,13 @@ std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
     if (I.p.framework == 0 && I.xs.n) tile_sketches(I, s);  // derived layout, not stored
     uint64_t want = r.h, got = 0;
     if (fread(&got, 1, 8, f) != 8 || got != want) throw Error(LSHG_ERR_IO, "index file checksum mismatch");
+    if (I.cp_diag.n) {  // the cross-polytope kernel applies the diagonals as sign flips
+      std::vector<int32_t> dg(I.cp_diag.n);
+      LSHG_CUDA(cudaMemcpyAsync(dg.data(), I.cp_diag.ptr, I.cp_diag.bytes(), cudaMemcpyDeviceToHost, s));
+      LSHG_CUDA(cudaStreamSynchronize(s));
+      for (int32_t g : dg)
+        if (g != 1 && g != -1) throw Error(LSHG_ERR_IO, "index file: cross-polytope diagonal entry is not +-1");
+    }
   } catch (...) {
     fclose(f);
     throw;
