@@ -38,7 +38,7 @@ __device__ __forceinline__ float times_sign(float v, int g) {
 // a warp usually share a table and its diagonals.
 // vec: d % 4 == 0 and 16-byte aligned rows -- chunks are read as 16-byte loads.
 template <int W>  // values a lane holds: 32 (P >= 32) or P
-__global__ void __launch_bounds__(256) crosspoly_kernel(const float* __restrict__ x, int64_t n, int d, int P,
+__global__ void __launch_bounds__(256, W == 32 ? 3 : 1) crosspoly_kernel(const float* __restrict__ x, int64_t n, int d, int P,
                                                         int tables, int hashes, int rounds,
                                                         const int* __restrict__ diag, uint16_t* __restrict__ keys,
                                                         bool vec) {
