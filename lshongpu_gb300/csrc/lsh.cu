@@ -420,19 +420,33 @@ __device__ __forceinline__ void seen_clear(int* seen, int tid) {
 // repeats in the CTA's shared-memory id set and write the distinct ids to
 // cand[q][0..cap); ccnt[q] = distinct count (a query with more than cap is listed in ovf
 // for the fused kernel, and its walk stops there).  No scoring state and no global
-// atomics: one barrier a round, and the set is cleared with 16-byte shared stores.
+// atomics on the entries: one barrier a round, and the set is cleared with 16-byte shared
+// stores.  CTAs take queries off the batch counter *qctr (zero at launch), so the batch's
+// uneven queries spread evenly over them.
 __global__ void __launch_bounds__(kQThreads, kWalkCtasPerSm)
-    lsh_walk_kernel(LshQueryArgs a, int* __restrict__ cand, int cap, int* __restrict__ ccnt, int* __restrict__ ovf) {
+    lsh_walk_kernel(LshQueryArgs a, int* __restrict__ cand, int cap, int* __restrict__ ccnt, int* __restrict__ ovf,
+                    int* __restrict__ qctr) {
   extern __shared__ __align__(16) int seen[];  // kWalkSlots ids
   __shared__ int bstart[kMaxTables], pref[kMaxTables + 1];
-  __shared__ int wcnt;
+  __shared__ int wcnt, qcur;
   const int tid = threadIdx.x, lane = tid & 31;
   seen_clear(seen, tid);
-  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
-    // the previous query's last reads of bstart/pref/wcnt precede its closing barrier
-    if (tid < 32) bucket_bounds_warp(a, qi, bstart, pref, lane);
-    if (tid == 0) wcnt = 0;
+  for (;;) {
+    // warp 0 takes the next query and loads its bucket bounds; the previous query's last
+    // reads of qcur/bstart/pref/wcnt precede its closing barrier
+    if (tid < 32) {
+      int q = 0;
+      if (lane == 0) q = atomicAdd(qctr, 1);
+      q = __shfl_sync(0xffffffffu, q, 0);
+      if (q < a.nq) bucket_bounds_warp(a, q, bstart, pref, lane);
+      if (lane == 0) {
+        qcur = q;
+        wcnt = 0;
+      }
+    }
     __syncthreads();
+    const int qi = qcur;
+    if (qi >= a.nq) break;
     const int total = pref[a.tables];
     int* dst = cand + (int64_t)qi * cap;
     for (int base = 0; base < total; base += kRound) {
@@ -490,11 +504,11 @@ __global__ void __launch_bounds__(kQThreads, kWalkCtasPerSm)
 
 // Split path, step 2: score each listed query's distinct candidates (rows staged by bulk
 // copies, staged_key) into its top-C and write the first k.  Queries whose lists
-// overflowed are left to the fused kernel.
+// overflowed are left to the fused kernel.  Queries come off the batch counter *qctr.
 template <int DIST>
 __global__ void __launch_bounds__(kQThreads, kScoreCtasPerSm)
     lsh_score_kernel(LshQueryArgs a, const int* __restrict__ cand, int cap, const int* __restrict__ ccnt,
-                     lshg_point* __restrict__ out) {
+                     lshg_point* __restrict__ out, int* __restrict__ qctr) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int NW = kQThreads / 32;
   const uint32_t stage_slot = stage_slot_bytes(a.d);
@@ -515,7 +529,12 @@ __global__ void __launch_bounds__(kQThreads, kScoreCtasPerSm)
   if (tid < NW) tc::mbar_init(tc::smem_u32(&stage_bar[tid]), 1);
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   __syncthreads();
-  for (int qi = blockIdx.x; qi < a.nq; qi += gridDim.x) {
+  __shared__ int qslot[2];  // alternate slots: thread 0 fills the next before all read the last
+  for (int it = 0;; ++it) {
+    if (tid == 0) qslot[it & 1] = atomicAdd(qctr, 1);  // queries come off the batch counter
+    __syncthreads();
+    const int qi = qslot[it & 1];
+    if (qi >= a.nq) break;
     const int c = ccnt[qi];
     if (c > cap) continue;  // uniform: the fused kernel answers this query
     for (int j = tid; j < dpad; j += kQThreads) qr[j] = j < a.d ? a.q[(int64_t)qi * a.d + j] : 0.0f;
@@ -624,9 +643,12 @@ void lsh_query_plan(LshQueryArgs& a, int max_grid) {
 
 template <int DV>
 static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg_point* out, cudaStream_t s) {
-  DevBuf<int> cand((size_t)a.nq * cap, s), ccnt((size_t)a.nq, s), ovf((size_t)a.nq + 1, s);
-  LSHG_CUDA(cudaMemsetAsync(ovf.ptr, 0, sizeof(int), s));
-  lsh_walk_kernel<<<a.walk_grid, kQThreads, kWalkSlots * 4, s>>>(a, cand.ptr, cap, ccnt.ptr, ovf.ptr);
+  // ctl: [0] walk's query counter, [1] scoring query counter, [2] overflow count, then the
+  // overflowing queries (the fused kernel's query list starts at [2])
+  DevBuf<int> cand((size_t)a.nq * cap, s), ccnt((size_t)a.nq, s), ctl((size_t)a.nq + 3, s);
+  LSHG_CUDA(cudaMemsetAsync(ctl.ptr, 0, 3 * sizeof(int), s));
+  int* ovf = ctl.ptr + 2;
+  lsh_walk_kernel<<<a.walk_grid, kQThreads, kWalkSlots * 4, s>>>(a, cand.ptr, cap, ccnt.ptr, ovf, ctl.ptr);
   count_launch();
   LSHG_CHECK_LAUNCH();
   const size_t ssmem = lsh_stage_bytes(a.d) + (size_t)(a.C + kQBuf) * 8 + (size_t)((a.d + 3) & ~3) * 4 + 16;
@@ -634,11 +656,11 @@ static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg
   int per = 0;
   LSHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lsh_score_kernel<DV>, kQThreads, ssmem));
   const int sgrid = std::max(1, std::min(a.nq, num_sms() * std::max(1, per)));
-  lsh_score_kernel<DV><<<sgrid, kQThreads, ssmem, s>>>(a, cand.ptr, cap, ccnt.ptr, out);
+  lsh_score_kernel<DV><<<sgrid, kQThreads, ssmem, s>>>(a, cand.ptr, cap, ccnt.ptr, out, ctl.ptr + 1);
   count_launch();
   LSHG_CHECK_LAUNCH();
   LshQueryArgs f = a;  // queries with more than cap distinct candidates: the fused kernel
-  f.qlist = ovf.ptr;
+  f.qlist = ovf;
   f.bitmap_dirty = 1;
   DevBuf<int> lists((size_t)a.grid * kListCap, s);
   f.lists = lists.ptr;
