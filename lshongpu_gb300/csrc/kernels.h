@@ -134,6 +134,7 @@ struct LshQueryArgs {
   int walk_grid;              // set by lsh_query_plan: CTAs of the bucket-walk kernel (split path)
   int split_cap;              // set by lsh_query_plan: distinct ids a query the walk lists (0: fused path)
   int bitmap_dirty;           // internal: the fused kernel zeroes its bitmap before its first query
+  int* qctr;                  // internal: the fused kernel's query counter (zero at launch)
   const int* qlist;           // internal: queries to answer ([0] = count, then indices); nullptr = all
   int* lists;                 // internal: the fused kernel's distinct-id lists, [grid][list capacity]
 };

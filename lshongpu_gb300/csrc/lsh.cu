@@ -181,7 +181,7 @@ __device__ __forceinline__ int entry_table(const int* pref, int tables, int idx)
   return lo;
 }
 
-// One CTA answers queries qi = blockIdx.x, +gridDim.x, ...  Per query: (1) the bucket
+// A CTA answers the queries it takes off the batch counter a.qctr.  Per query: (1) the bucket
 // entries are walked kUnroll per thread per round, deduplicated, and distinct ids appended
 // to a shared list; (2) whenever the list holds kScoreAt ids (and after the last round)
 // they are scored, one thread per candidate, and offered to the top-C queue.  Scoring
@@ -221,11 +221,18 @@ __global__ void __launch_bounds__(kQThreads, kQueryCtasPerSm) lsh_query_kernel(L
   __syncthreads();
 
   const int nloop = a.qlist ? a.qlist[0] : a.nq;
-  if (a.bitmap_dirty && (int)blockIdx.x < nloop) {  // nobody zeroed the bitmap: do it once
-    for (int w = tid; w < (a.n + 31) / 32; w += kQThreads) bitmap[w] = 0u;
+  bool bitmap_zero = !a.bitmap_dirty;  // uniform
+  __shared__ int qslot[2];  // alternate slots: thread 0 fills the next before all read the last
+  for (int it = 0;; ++it) {
+    if (tid == 0) qslot[it & 1] = atomicAdd(a.qctr, 1);  // queries come off the batch counter
     __syncthreads();
-  }
-  for (int ii = blockIdx.x; ii < nloop; ii += gridDim.x) {
+    const int ii = qslot[it & 1];
+    if (ii >= nloop) break;
+    if (!bitmap_zero) {  // nobody zeroed the bitmap: do it before the CTA's first query
+      for (int w = tid; w < (a.n + 31) / 32; w += kQThreads) bitmap[w] = 0u;
+      __syncthreads();
+      bitmap_zero = true;
+    }
     const int qi = a.qlist ? a.qlist[1 + ii] : ii;
     for (int j = tid; j < dpad; j += kQThreads) qr[j] = j < a.d ? a.q[(int64_t)qi * a.d + j] : 0.0f;
     if (a.sketched) {
@@ -643,11 +650,11 @@ void lsh_query_plan(LshQueryArgs& a, int max_grid) {
 
 template <int DV>
 static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg_point* out, cudaStream_t s) {
-  // ctl: [0] walk's query counter, [1] scoring query counter, [2] overflow count, then the
-  // overflowing queries (the fused kernel's query list starts at [2])
-  DevBuf<int> cand((size_t)a.nq * cap, s), ccnt((size_t)a.nq, s), ctl((size_t)a.nq + 3, s);
-  LSHG_CUDA(cudaMemsetAsync(ctl.ptr, 0, 3 * sizeof(int), s));
-  int* ovf = ctl.ptr + 2;
+  // ctl: query counters of the walk [0], the scoring [1] and the fused kernel [2]; [3] the
+  // overflow count, then the overflowing queries (the fused kernel's query list starts at [3])
+  DevBuf<int> cand((size_t)a.nq * cap, s), ccnt((size_t)a.nq, s), ctl((size_t)a.nq + 4, s);
+  LSHG_CUDA(cudaMemsetAsync(ctl.ptr, 0, 4 * sizeof(int), s));
+  int* ovf = ctl.ptr + 3;
   lsh_walk_kernel<<<a.walk_grid, kQThreads, kWalkSlots * 4, s>>>(a, cand.ptr, cap, ccnt.ptr, ovf, ctl.ptr);
   count_launch();
   LSHG_CHECK_LAUNCH();
@@ -662,6 +669,7 @@ static void launch_split(const LshQueryArgs& a, int cap, size_t fused_smem, lshg
   LshQueryArgs f = a;  // queries with more than cap distinct candidates: the fused kernel
   f.qlist = ovf;
   f.bitmap_dirty = 1;
+  f.qctr = ctl.ptr + 2;
   DevBuf<int> lists((size_t)a.grid * kListCap, s);
   f.lists = lists.ptr;
   LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem));
@@ -689,9 +697,11 @@ void launch_lsh_query(const LshQueryArgs& a, lshg_point* out, cudaStream_t s) {
     }
     return;
   }
-  DevBuf<int> lists((size_t)a.grid * kListCap, s);
+  DevBuf<int> lists((size_t)a.grid * kListCap, s), qctr(1, s);
+  LSHG_CUDA(cudaMemsetAsync(qctr.ptr, 0, sizeof(int), s));
   LshQueryArgs f = a;
   f.lists = lists.ptr;
+  f.qctr = qctr.ptr;
 #define LSHG_LQ(DV)                                                                                        \
   do {                                                                                                     \
     LSHG_CUDA(cudaFuncSetAttribute(lsh_query_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
