@@ -53,6 +53,7 @@ constexpr int F_TMEM_COLS = F_NACC * TN;        // 512 = all of TMEM (one CTA pe
 constexpr int F_EPI_WARPS = 16;  // four warpgroups, one 64-column piece each
 
 constexpr int F_SBUF = 8;  // staged survivors a row and warpgroup (flushed with one atomic)
+constexpr int kTauRegs = 80;  // group maxima a lane holds in the register threshold select
 
 // Shared-memory layout by operand format.  BF16: a tile row is two 128-byte swizzle rows
 // (64 columns each); E4M3: one (all 128 columns), so tiles are half the size and the
@@ -327,6 +328,42 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   if (threadIdx.x == 0 && *abort_flag) atomicExch(a.err, 2);
 }
 
+// Descending scan of one warp's 256-bin histogram: digit = the bin where the count of keys
+// in bins >= digit first reaches kk, rem = kk minus the count in the bins above it.  Lane l
+// owns bins 255-8l .. 248-8l.  False (digit, rem untouched) when the bins hold fewer than
+// kk keys.
+__device__ __forceinline__ bool digit_of_rank(const unsigned* hist, int kk, int lane, int& digit, int& rem) {
+  unsigned own = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) own += hist[255 - 8 * lane - j];
+  unsigned incl = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (__shfl_sync(0xffffffffu, incl, 31) < (unsigned)kk) return false;
+  const unsigned hit = __ballot_sync(0xffffffffu, incl >= (unsigned)kk);
+  const int L = __ffs(hit) - 1;
+  int dg = 0, rm = 0;
+  if (lane == L) {
+    unsigned acc = incl - own;
+    for (int j = 0; j < 8; ++j) {
+      const int d = 255 - 8 * lane - j;
+      const unsigned h = hist[d];
+      if (acc + h >= (unsigned)kk) {
+        dg = d;
+        rm = kk - (int)acc;
+        break;
+      }
+      acc += h;
+    }
+  }
+  digit = __shfl_sync(0xffffffffu, dg, L);
+  rem = __shfl_sync(0xffffffffu, rm, L);
+  return true;
+}
+
 // tau[q] = (CT-th largest of the row's M group maxima) - margin, or -inf when the row has
 // fewer than CT finite-or-infinite (non-NaN) maxima.  One warp per query: a 4-pass
 // 8-bit radix select on order-preserving keys, histogram in shared memory.
@@ -349,45 +386,74 @@ __global__ void __launch_bounds__(256) tau_select_kernel(const float* __restrict
       if ((key & pmask) == prefix) atomicAdd(&hist[w][(key >> shift) & 255u], 1u);
     }
     __syncwarp();
-    // lane l owns digits 255-8l .. 248-8l (descending); inclusive prefix over lanes
-    unsigned own = 0;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) own += hist[w][255 - 8 * lane - j];
-    unsigned incl = own;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total < (unsigned)kk) {  // fewer than CT usable maxima (only possible on the first pass)
+    int digit = 0, rem = 0;
+    if (!digit_of_rank(hist[w], kk, lane, digit, rem)) {  // fewer than CT usable maxima (first pass only)
       if (lane == 0) tau[q] = -INFINITY;
       return;
     }
-    const unsigned hit = __ballot_sync(0xffffffffu, incl >= (unsigned)kk);
-    const int L = __ffs(hit) - 1;
-    int digit = 0, rem = 0;
-    if (lane == L) {
-      unsigned acc = incl - own;
-      for (int j = 0; j < 8; ++j) {
-        const int d = 255 - 8 * lane - j;
-        const unsigned h = hist[w][d];
-        if (acc + h >= (unsigned)kk) {
-          digit = d;
-          rem = kk - (int)acc;
-          break;
-        }
-        acc += h;
-      }
-    }
-    digit = __shfl_sync(0xffffffffu, digit, L);
-    rem = __shfl_sync(0xffffffffu, rem, L);
     prefix |= (uint32_t)digit << shift;
     pmask |= 255u << shift;
     kk = rem;
     __syncwarp();
   }
   if (lane == 0) tau[q] = ordered_to_float(prefix) - margin;
+}
+
+// tau_select_kernel for rows of at most 32 * R maxima (a multiple of 4), read once into
+// registers by 16-byte loads.  It
+// returns a lower bound of the CT-th largest maximum (minus the margin), which is all the
+// filter needs -- a lower threshold only keeps more survivors, and the candidates
+// selected from them are the same: a bisection on the order-preserving key between the
+// row's smallest and largest maximum above -inf keeps lo with at least CT keys >= lo (so
+// lo never passes the CT-th largest) and stops at 1/65536 of the range; each probe is a
+// compare a key and one warp reduction (no histogram atomics, whose bins the clustered
+// keys share).  With fewer than CT maxima above -inf (NaN is not a score) the CT-th
+// largest is -inf, and so is tau, as in the exact select.
+template <int R>
+__global__ void __launch_bounds__(256) tau_select_reg_kernel(const float* __restrict__ gmax, int nq, int M, int CT,
+                                                              float margin, float* __restrict__ tau) {
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (q >= nq) return;  // warp-uniform
+  // all R/4 16-byte loads issued before any is used (M % 4 == 0: rows are 16-byte aligned)
+  const float4* row = reinterpret_cast<const float4*>(gmax + (int64_t)q * M);
+  float4 raw[R / 4];
+#pragma unroll
+  for (int j = 0; j < R / 4; ++j) {
+    const int i4 = j * 32 + lane;
+    raw[j] = 4 * i4 < M ? __ldg(row + i4) : make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY);
+  }
+  uint32_t key[R];  // ordered keys; 0 = no value (no float but a NaN maps to 0)
+  int valid = 0;
+  uint32_t kmax = 0u, kmin = 0xffffffffu;
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const float4 r4 = raw[j / 4];
+    const float f = (j & 3) == 0 ? r4.x : (j & 3) == 1 ? r4.y : (j & 3) == 2 ? r4.z : r4.w;
+    key[j] = (f == f && f != -INFINITY) ? float_to_ordered(f) : 0u;
+    if (key[j]) {
+      ++valid;
+      kmax = max(kmax, key[j]);
+      kmin = min(kmin, key[j]);
+    }
+  }
+  if (__reduce_add_sync(0xffffffffu, valid) < CT) {
+    if (lane == 0) tau[q] = -INFINITY;
+    return;
+  }
+  kmax = __reduce_max_sync(0xffffffffu, kmax);
+  kmin = __reduce_min_sync(0xffffffffu, kmin);
+  uint64_t lo = kmin, hi = (uint64_t)kmax + 1;  // count(>= lo) >= CT > count(>= hi)
+  const uint64_t stop = ((hi - lo) >> 16) + 1;
+  while (hi - lo > stop) {  // warp-uniform
+    const uint32_t mid = (uint32_t)(lo + ((hi - lo) >> 1));
+    int c = 0;
+#pragma unroll
+    for (int j = 0; j < R; ++j) c += key[j] >= mid ? 1 : 0;  // empty slots (0) never count: mid >= kmin >= 1
+    if (__reduce_add_sync(0xffffffffu, c) >= CT) lo = mid;
+    else hi = mid;
+  }
+  if (lane == 0) tau[q] = ordered_to_float((uint32_t)lo) - margin;
 }
 
 // Per query (one warp): the CT = 32*E smallest keys of the survivors -- sort each chunk of
@@ -560,7 +626,10 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
     }
     {
       ProfScope _ps("tc_tau_select", s);
-      tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, margin, tau);
+      if (plan.M <= 32 * kTauRegs && plan.M % 4 == 0)
+        tau_select_reg_kernel<kTauRegs><<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, margin, tau);
+      else
+        tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, margin, tau);
       count_launch();
       LSHG_CHECK_LAUNCH();
     }
