@@ -47,6 +47,30 @@ def test_crosspoly_keys_buckets_query(engine, orc, hashes, bits):
     assert np.array_equal(res["distance"], ds)
 
 
+@pytest.mark.parametrize("d", [5, 16, 30, 64, 99, 200, 513])
+def test_crosspoly_keys_every_lane_layout(engine, orc, d):
+    """Base and query keys bit-identical to the oracle for every lane layout of the key
+    kernel: P < 32 (a unit in one lane: P = 8, 16), P = 32 (one lane, four-float chunks),
+    units spread over 2 .. 32 lanes (P = 64 .. 1024), 16-byte loads (d % 4 == 0) and
+    scalar loads, one and two rotations a key."""
+    P = 1 << (d - 1).bit_length()
+    n, nq, L = 1500, 16, 4
+    x = datasets.clustered(n, d, 71, count=12)
+    q = datasets.clustered(nq, d, 72, count=12)
+    xn, qn = orc.normalize(x), orc.normalize(q)
+    for hashes in (1, 2):
+        if (2 * P) ** hashes > 65536:
+            continue
+        bits = max(8, ((2 * P) ** hashes - 1).bit_length())
+        idx = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7,
+                           bucketKeyBits=bits, tables=L, options=engine.make_options(cp_hashes=hashes))
+        diag = engine.random_plus_minus(P * L * 3 * hashes)
+        keys, _, _ = lsh_index_arrays(engine, idx, n, L, 1 << bits)
+        assert np.array_equal(keys, orc.crosspoly(xn, P, L, hashes, 3, diag)), (d, hashes)
+        _, qk = idx.sketch_queries(q, np.uint32, 0, L)
+        assert np.array_equal(qk, orc.crosspoly(qn, P, L, hashes, 3, diag)), (d, hashes)
+
+
 def walked_and_distinct(qkeys, off, bk, tables, S, n):
     """Bucket entries each query walks and its distinct candidates, from the oracle's tables."""
     ent, dis = [], []
