@@ -103,15 +103,16 @@ __global__ void __launch_bounds__(256, W == 32 ? 3 : 1) crosspoly_kernel(const f
           }
         }
         // offsets 2G .. 4: lane bits, partner lane j ^ o/4 of the group.  The lower lane
-        // keeps other + v and the upper one other - v = other + (-v): IEEE addition
-        // commutes and subtraction is addition of the negation, so both are one rounded
-        // add of the same operands as the reference's a + b and a - b.
+        // keeps other + v and the upper one other - v, both as fma(v, +-1, other): v * +-1
+        // is exact and the fma rounds once, so the result is the rounded sum other + (+-v)
+        // -- IEEE addition commutes and subtraction is addition of the negation, so it is
+        // the reference's a + b or a - b bit for bit.
         for (int lo = G >> 1; lo > 0; lo >>= 1) {
-          const int flip = (j & lo) ? -1 : 1;
+          const float sgn = (j & lo) ? -1.0f : 1.0f;
 #pragma unroll
           for (int e = 0; e < W; ++e) {
             const float other = __shfl_xor_sync(0xffffffffu, v[e], lo);
-            v[e] = __fadd_rn(other, times_sign(v[e], flip));
+            v[e] = __fmaf_rn(v[e], sgn, other);
           }
         }
         // offsets 2, 1: bits of r, inside a chunk
