@@ -54,11 +54,50 @@ __device__ __forceinline__ void warp_bitonic_merge(uint64_t* a, int n) {
   }
 }
 
-// Block-cooperative ascending bitonic sort of n (power of two) keys in shared memory.
-// Every thread of the block must call it.
+// One compare-exchange stage of a bitonic network on the 32 keys of a warp's registers
+// (lane l holds element c*32 + l): partners are lanes l and l ^ s (s < 32); `up` (from the
+// element index and the block size being sorted) says whether the lower index keeps the
+// smaller key.  Same result as the shared-memory stage below.
+__device__ __forceinline__ uint64_t bitonic_lane_stage(uint64_t x, int s, bool up, int lane) {
+  const uint64_t y = __shfl_xor_sync(0xffffffffu, x, s);
+  const bool keep_min = ((lane & s) == 0) == up;
+  return keep_min ? (x < y ? x : y) : (x < y ? y : x);
+}
+
+// Block-cooperative ascending bitonic sort of n (power of two) keys in shared memory;
+// every thread of the block (a whole number of warps) must call it.  Stages with stride >= 32 run in shared memory (a warp's pairs are 32 consecutive keys:
+// no bank conflicts); each size's stages with stride < 32 run in registers on 32-key
+// chunks, one chunk a warp, with shuffles -- one load, up to five exchanges and one store
+// instead of five shared-memory passes with 2-way conflicts and a barrier each.
 __device__ __forceinline__ void block_bitonic_sort(uint64_t* a, int n) {
-  for (int size = 2; size <= n; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+  if (n < 64) {  // small lists: the plain network
+    for (int size = 2; size <= n; size <<= 1) {
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
+          int i = 2 * t - (t & (stride - 1));
+          int j = i + stride;
+          bool up = ((i & size) == 0);
+          uint64_t x = a[i], y = a[j];
+          if ((x > y) == up) { a[i] = y; a[j] = x; }
+        }
+        __syncthreads();
+      }
+    }
+    return;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int c = warp; c < (n >> 5); c += nw) {  // sizes 2 .. 32: all inside a 32-key chunk
+    const int i = c * 32 + lane;
+    uint64_t x = a[i];
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1)
+#pragma unroll
+      for (int s = size >> 1; s > 0; s >>= 1) x = bitonic_lane_stage(x, s, (i & size) == 0, lane);
+    a[i] = x;
+  }
+  __syncthreads();
+  for (int size = 64; size <= n; size <<= 1) {
+    for (int stride = size >> 1; stride >= 32; stride >>= 1) {
       for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
         int i = 2 * t - (t & (stride - 1));
         int j = i + stride;
@@ -68,12 +107,23 @@ __device__ __forceinline__ void block_bitonic_sort(uint64_t* a, int n) {
       }
       __syncthreads();
     }
+    for (int c = warp; c < (n >> 5); c += nw) {  // strides 16 .. 1 of this size
+      const int i = c * 32 + lane;
+      const bool up = (i & size) == 0;  // the same for the whole chunk (size >= 64)
+      uint64_t x = a[i];
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) x = bitonic_lane_stage(x, s, up, lane);
+      a[i] = x;
+    }
+    __syncthreads();
   }
 }
 
-// Block-cooperative ascending sort of a bitonic sequence of n (power of two) keys.
+// Block-cooperative ascending sort of a bitonic sequence of n (power of two) keys; strides
+// below 32 in registers as in block_bitonic_sort.
 __device__ __forceinline__ void block_bitonic_merge(uint64_t* a, int n) {
-  for (int stride = n >> 1; stride > 0; stride >>= 1) {
+  const int reg_below = n >= 64 ? 32 : 0;
+  for (int stride = n >> 1; stride > 0 && stride >= reg_below; stride >>= 1) {
     for (int t = threadIdx.x; t < (n >> 1); t += blockDim.x) {
       int i = 2 * t - (t & (stride - 1));
       int j = i + stride;
@@ -82,6 +132,16 @@ __device__ __forceinline__ void block_bitonic_merge(uint64_t* a, int n) {
     }
     __syncthreads();
   }
+  if (reg_below == 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int c = warp; c < (n >> 5); c += nw) {
+    const int i = c * 32 + lane;
+    uint64_t x = a[i];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) x = bitonic_lane_stage(x, s, true, lane);
+    a[i] = x;
+  }
+  __syncthreads();
 }
 
 // Fold an unsorted buffer of `cnt` keys into the sorted kept list of C keys (C a power
