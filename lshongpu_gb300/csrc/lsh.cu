@@ -6,14 +6,17 @@
 // point ids with atomic cursors (:126-140).  Order inside a bucket is the atomic order,
 // as in the reference; nothing downstream depends on it and exports sort it.
 //
-// Query (scan, :142-252 + removeDuplicates, :255-280): one CTA per query gathers the
-// ids of its L buckets (bucket t ends at the next key's offset, or at the table's end
-// for the last key, :183-184), drops repeats with a per-CTA bitmap (the reference keeps
-// repeats in its queue and removes adjacent equal ids after sorting), scores each
-// distinct candidate exactly or by sketch, keeps the best C by (distance, id), and for
-// sketched scoring re-ranks them exactly (candidateSetScan, :236-238) before writing the
-// first k.  Fewer than k distinct candidates leave (-1, INT_MAX) entries.  Exact scoring
-// stages candidate rows in shared memory with bulk copies (see staged_key).
+// Query (scan, :142-252 + removeDuplicates, :255-280): a CTA per query gathers the ids
+// of its L buckets (bucket t ends at the next key's offset, or at the table's end for
+// the last key, :183-184), drops repeats (the reference keeps repeats in its queue and
+// removes adjacent equal ids after sorting), scores each distinct candidate exactly or by
+// sketch, keeps the best C by (distance, id), and for sketched scoring re-ranks them
+// exactly (candidateSetScan, :236-238) before writing the first k.  Fewer than k distinct
+// candidates leave (-1, INT_MAX) entries.  Exact scoring with staged rows runs as two
+// kernels: lsh_walk_kernel drops repeats in a shared-memory id set and lists each
+// query's distinct ids, lsh_score_kernel scores the lists with rows staged in shared
+// memory by bulk copies (staged_key).  Sketched scoring, and queries whose lists
+// overflow, run the fused lsh_query_kernel, which drops repeats with a per-CTA bitmap.
 #include "common.cuh"
 #include "distance.cuh"
 #include "kernels.h"
