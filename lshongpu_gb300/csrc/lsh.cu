@@ -38,11 +38,11 @@ constexpr int kScoreAt = 1024;                // score the distinct list once it
 constexpr int kListCap = kScoreAt + kRound;   // a round adds at most kRound ids
 constexpr int kStageRows = 16;                // rows a warp stages per bulk-copy batch
 constexpr int kStageMaxBytes = 136 * 1024;    // staging area limit (d up to 268 at 16 rows x 8 warps)
-constexpr int kWalkCtasPerSm = 3;             // bucket-walk CTAs an SM (split path; 64 KB id set each)
-constexpr int kWalkSlotBits = 14;
-constexpr int kWalkSlots = 1 << kWalkSlotBits;  // slots of a walk CTA's shared id set
-constexpr int kSplitCap = 8192;               // distinct candidates a query listed by the walk
-static_assert(kSplitCap + kRound <= kWalkSlots * 5 / 8, "walk id set: load factor at most 5/8");
+constexpr int kWalkCtasPerSm = 4;             // bucket-walk CTAs an SM (split path; 48 KB id set each)
+constexpr int kWalkSlots = 12288;             // slots of a walk CTA's shared id set
+constexpr int kSplitCap = 6144;               // distinct candidates a query listed by the walk
+static_assert(3 * (kSplitCap + kRound) <= 2 * kWalkSlots, "walk id set: load factor at most 2/3");
+static_assert(kWalkSlots % 4 == 0, "walk id set: cleared with 16-byte stores");
 constexpr int kScoreCtasPerSm = 3;            // scoring CTAs an SM (register budget: 80 a thread)
 constexpr int kQueryCtasPerSm = 3;            // resident fused-kernel CTAs an SM (register budget;
                                               // d = 128 staging, 66 KB a CTA, allows three)
@@ -408,16 +408,16 @@ __device__ __forceinline__ void bucket_bounds_warp(const LshQueryArgs& a, int qi
 }
 
 // Open-addressing set of point ids in shared memory (kWalkSlots slots, -1 = empty, linear
-// probing from a Fibonacci hash).  True when id was absent.  The walk inserts at most
-// cap + kRound ids a query, well below kWalkSlots, so a free slot is always found; the
-// probe count is bounded all the same.
+// probing from a Fibonacci hash mapped onto the slots by a multiply-shift).  True when id
+// was absent.  The walk inserts at most cap + kRound ids a query, at most 2/3 of
+// kWalkSlots, so a free slot is always found; the probe count is bounded all the same.
 __device__ __forceinline__ bool seen_insert(int* seen, int id) {
-  uint32_t h = ((uint32_t)id * 2654435769u) >> (32 - kWalkSlotBits);
+  uint32_t h = (uint32_t)(((uint64_t)((uint32_t)id * 2654435769u) * (uint32_t)kWalkSlots) >> 32);
   for (int p = 0; p < kWalkSlots; ++p) {
     const int prev = atomicCAS(&seen[h], -1, id);
     if (prev == -1) return true;
     if (prev == id) return false;
-    h = (h + 1) & (kWalkSlots - 1);
+    h = h + 1 == (uint32_t)kWalkSlots ? 0u : h + 1;
   }
   return false;
 }
