@@ -9,6 +9,7 @@ from lshongpu_gb300 import datasets
 pytestmark = pytest.mark.gpu
 
 D = 100
+WALK_LIST_CAP = 6144  # distinct ids a query the bucket walk lists (kSplitCap in csrc/lsh.cu)
 
 
 def data(n, nq, seed=21):
@@ -106,7 +107,7 @@ def test_crosspoly_many_candidates_and_counters(engine, orc, d, P):
     oqk = orc.crosspoly(qn, P, L, 1, 3, diag)
     ooff, obk = orc.lsh_build(okeys, L, S)
     ent, dis = walked_and_distinct(oqk, ooff, obk, L, S, n)
-    assert dis.min() > 8192  # the case this test is for
+    assert dis.min() > WALK_LIST_CAP  # the case this test is for
     assert idx.query_counters() == (0, 0)
     res = idx.query(q, 32)
     ids, ds = orc.lsh_query(xn, qn, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, 1, 32)
@@ -116,10 +117,11 @@ def test_crosspoly_many_candidates_and_counters(engine, orc, d, P):
 
 
 def test_crosspoly_mixed_list_sizes_one_batch(engine, orc):
-    """One batch where 24 queries (in a 30,000-point cluster) have more distinct candidates
-    than the bucket walk lists and go through the fused kernel, and 40 (among 2,000 small
-    clusters) have a few hundred to a few thousand and are scored from their lists; both
-    halves must equal the oracle and the counters the oracle's totals."""
+    """One batch where 25 queries (24 in a 30,000-point cluster, one of the small-cluster
+    ones) have more distinct candidates than the bucket walk lists and go through the fused
+    kernel, and 39 (among 2,000 small clusters) have a few hundred to a few thousand and are
+    scored from their lists; both parts must equal the oracle and the counters the oracle's
+    totals."""
     d, P, L, bits, n = D, 128, 12, 8, 40000
     x = np.concatenate([datasets.clustered(30000, d, 71, count=1, center_seed=55),
                         datasets.clustered(10000, d, 72, count=2000, center_seed=56)])
@@ -133,7 +135,7 @@ def test_crosspoly_mixed_list_sizes_one_batch(engine, orc):
     oqk = orc.crosspoly(qn, P, L, 1, 3, diag)
     ooff, obk = orc.lsh_build(orc.crosspoly(xn, P, L, 1, 3, diag), L, S)
     ent, dis = walked_and_distinct(oqk, ooff, obk, L, S, n)
-    assert (dis > 8192).sum() == 24 and (dis <= 8192).sum() == 40  # the case this test is for
+    assert (dis > WALK_LIST_CAP).sum() == 25 and (dis <= WALK_LIST_CAP).sum() == 39  # the case this test is for
     res = idx.query(q, 32)
     ids, ds = orc.lsh_query(xn, qn, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, 1, 32)
     assert np.array_equal(res["ID"], ids)
