@@ -255,6 +255,7 @@ int lshg_index_query(lshg_index* idx, const float* queries, int N_query, int k, 
   return guarded([&] {
     LSHG_REQUIRE(idx && results && (queries || N_query == 0), "NULL argument");
     Index& I = *idx->impl;
+    check_device(I);
     cudaStream_t s = stream ? (cudaStream_t)stream : I.stream;
     DevBuf<float> q((size_t)N_query * I.d, s);
     if (N_query)
@@ -278,6 +279,7 @@ int lshg_index_query_async(lshg_index* idx, const float* queries, int N_query, i
   return guarded([&] {
     LSHG_REQUIRE(idx && results && (queries || N_query == 0), "NULL argument");
     Index& I = *idx->impl;
+    check_device(I);
     cudaStream_t s = stream ? (cudaStream_t)stream : I.stream;
     // the pipelines preprocess queries in place: work on a stream-ordered copy
     DevBuf<float> q((size_t)N_query * I.d, s);
@@ -299,6 +301,7 @@ int lshg_index_sync(lshg_index* idx, void* stream) {
   return guarded([&] {
     LSHG_REQUIRE(idx, "NULL argument");
     Index& I = *idx->impl;
+    check_device(I);
     cudaStream_t s = stream ? (cudaStream_t)stream : I.stream;
     LSHG_CUDA(cudaStreamSynchronize(s));
     query_error(I, s);
@@ -306,13 +309,23 @@ int lshg_index_sync(lshg_index* idx, void* stream) {
 }
 
 int lshg_index_free(lshg_index* idx) {
-  return guarded([&] { delete idx; });
+  return guarded([&] {
+    if (!idx) return;
+    // release on the index's device, whatever the calling thread's current device is
+    int cur = -1;
+    LSHG_CUDA(cudaGetDevice(&cur));
+    const int dev = idx->impl ? idx->impl->device : cur;
+    if (dev != cur) LSHG_CUDA(cudaSetDevice(dev));
+    delete idx;
+    if (dev != cur) LSHG_CUDA(cudaSetDevice(cur));
+  });
 }
 
 int lshg_index_export(lshg_index* idx, int what, void* dst, size_t* bytes) {
   return guarded([&] {
     LSHG_REQUIRE(idx && bytes, "NULL argument");
     Index& I = *idx->impl;
+    check_device(I);
     cudaStream_t s = I.stream;
     const void* src = nullptr;
     size_t nb = 0;
@@ -364,6 +377,7 @@ int lshg_index_sketch_queries(lshg_index* idx, const float* queries, int N_query
   return guarded([&] {
     LSHG_REQUIRE(idx && queries, "NULL argument");
     Index& I = *idx->impl;
+    check_device(I);
     cudaStream_t s = I.stream;
     DevBuf<float> q = upload_floats(queries, (size_t)N_query * I.d, s);
     DevBuf<uint32_t> qs;

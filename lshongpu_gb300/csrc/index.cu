@@ -244,11 +244,31 @@ struct EventTimer {
 
 }  // namespace
 
+int* Index::error_word(cudaStream_t s) {
+  std::lock_guard<std::mutex> g(err_mu);
+  auto it = err_words.find(s);
+  if (it != err_words.end()) return it->second;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  LSHG_CUDA(cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone)
+    throw Error(LSHG_ERR_INVALID_ARGUMENT,
+                "first query of an index on this stream during a stream capture: run one query on the stream first");
+  int* w = nullptr;
+  LSHG_CUDA(cudaMalloc(&w, sizeof(int)));
+  if (cudaMemsetAsync(w, 0, sizeof(int), s) != cudaSuccess) {
+    cudaFree(w);
+    LSHG_CUDA(cudaGetLastError());
+  }
+  err_words.emplace(s, w);
+  return w;
+}
+
 Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
+  for (auto& kv : err_words) cudaFree(kv.second);  // cudaFree waits for work that may still write it
   x.release(); xnorm.release(); xt.release(); xs.release(); xsf.release(); xsft.release(); sk_planes.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
-  xbf.release(); xbf_scale.release(); xf8.release(); xst.release(); qerr.release(); qstats.release();
+  xbf.release(); xbf_scale.release(); xf8.release(); xst.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();
@@ -279,8 +299,6 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
   I.C = std::min(4096, std::max(32, next_pow2(C)));
   DevBuf<int> err(1, s);
   LSHG_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(int), s));
-  I.qerr.alloc(1, s);
-  LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
   I.qstats.alloc(2, s);
   LSHG_CUDA(cudaMemsetAsync(I.qstats.ptr, 0, I.qstats.bytes(), s));
   EventTimer tm(s);
@@ -440,18 +458,28 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
 
 void sketch_queries(Index& I, float* q, int nq, DevBuf<uint32_t>* qs, DevBuf<float>* qsf, DevBuf<uint16_t>* qkeys,
                     cudaStream_t s) {
+  int* err = I.error_word(s);
   apply_ops(I.ops_keys, q, nq, I.d, s);
-  if (I.p.framework == 1 && qkeys) make_keys(I, q, nq, qkeys, I.qerr.ptr, s);
+  if (I.p.framework == 1 && qkeys) make_keys(I, q, nq, qkeys, err, s);
   apply_ops(I.ops_sketch, q, nq, I.d, s);
-  if (I.sk_kind) make_sketch(I, q, nq, 0xff, qs, qsf, I.qerr.ptr, s);
+  if (I.sk_kind) make_sketch(I, q, nq, 0xff, qs, qsf, err, s);
+}
+
+void check_device(const Index& I) {
+  int dev = -1;
+  LSHG_CUDA(cudaGetDevice(&dev));
+  if (dev != I.device)
+    throw Error(LSHG_ERR_INVALID_ARGUMENT, "the index lives on device " + std::to_string(I.device) +
+                                               " but the calling thread's current device is " + std::to_string(dev));
 }
 
 void query_error(Index& I, cudaStream_t s) {
   int e = 0;
-  LSHG_CUDA(cudaMemcpyAsync(&e, I.qerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int* w = I.error_word(s);
+  LSHG_CUDA(cudaMemcpyAsync(&e, w, sizeof(int), cudaMemcpyDeviceToHost, s));
   LSHG_CUDA(cudaStreamSynchronize(s));
   if (e) {
-    LSHG_CUDA(cudaMemsetAsync(I.qerr.ptr, 0, sizeof(int), s));
+    LSHG_CUDA(cudaMemsetAsync(w, 0, sizeof(int), s));
     if (e == 2) throw Error(LSHG_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out (kernel aborted)");
     if (e == 3) throw Error(LSHG_ERR_TIMEOUT, "a row-copy wait timed out (the rows were re-read directly)");
     throw Error(LSHG_ERR_SAMPLER_LIMIT, "weighted MinHash sampler exceeded its draw limit (zero or NaN query?)");
@@ -508,7 +536,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     if (a.split_cap == 0) LSHG_CUDA(cudaMemsetAsync(bm.ptr, 0, bm.bytes(), s));
     a.bitmaps = bm.ptr;
     a.stats = I.qstats.ptr;
-    a.err = I.qerr.ptr;
+    a.err = I.error_word(s);
     launch_lsh_query(a, out, s);
     return;
   }
@@ -551,7 +579,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     launch_merge_splits(part.ptr, nq, splits, C, merged.ptr, s);
     cand = merged.ptr;
   }
-  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.qerr.ptr);
+  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s));
 }
 
 }  // namespace lshg

@@ -3,7 +3,9 @@
 // query batch.
 #pragma once
 
+#include <map>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -76,9 +78,16 @@ struct Index {
   DevBuf<uint8_t> xf8;       // E4M3 unit rows x kE4M3Scale, 128 bytes (implementation 9)
   int dp = 0;
 
-  // device error flag of the query path (weighted-MinHash draw limit); read by callers
-  // after the query has completed, so the query itself never synchronises
-  DevBuf<int> qerr;
+  // Device error words of the query path (a pipeline or row-copy wait that timed out,
+  // the weighted-MinHash draw limit), one per stream that has run queries on this index:
+  // the kernels of a batch raise the word of the stream they run on, and a sync on a
+  // stream reports and clears only that stream's word.  Read by callers after the query
+  // has completed, so the query itself never synchronises.
+  std::mutex err_mu;
+  std::map<cudaStream_t, int*> err_words;
+  // The stream's word, created (zeroed on the stream) by its first query.  Creating one
+  // inside a stream capture is refused: the first query on a stream must come before.
+  int* error_word(cudaStream_t s);
   // query counters (LSH: bucket entries walked, distinct candidates scored), cumulative
   DevBuf<unsigned long long> qstats;
 
@@ -97,8 +106,11 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
 // and no pageable copies, so it can be recorded into a CUDA graph; callers check
 // query_error() after the stream has completed.
 void query_index(Index& idx, float* q, int nq, int k, lshg_point* out, cudaStream_t stream);
-// Throws if the last completed query raised the device error flag (clears it).
+// Throws if a completed query on `stream` raised that stream's device error word (clears it).
 void query_error(Index& idx, cudaStream_t stream);
+// Throws LSHG_ERR_INVALID_ARGUMENT unless the calling thread's current device is the
+// device the index was built or loaded on.
+void check_device(const Index& idx);
 
 // Sketch / key a device query batch (after replaying the preprocessing).
 void sketch_queries(Index& idx, float* q, int nq, DevBuf<uint32_t>* qs, DevBuf<float>* qsf,

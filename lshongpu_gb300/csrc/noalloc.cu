@@ -18,7 +18,10 @@
 //    in the same call;
 //  * the first call on each device looks the array's device address up
 //    (cudaGetSymbolAddress, with that device current); make that first call before any
-//    stream capture begins.
+//    stream capture begins;
+//  * the calling thread's current device must be the index's device (the call is
+//    rejected with LSHG_ERR_INVALID_ARGUMENT otherwise), so the array used is the one on
+//    the GPU that holds the index.
 //  * batches whose temporaries exceed the array are rejected with
 //    LSHG_ERR_INVALID_ARGUMENT.
 #include <mutex>
@@ -36,10 +39,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 std::mutex g_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array for the current device (looked up once per device).
-void* scratch_for_current_device() {
-  int dev = 0;
-  LSHG_CUDA(cudaGetDevice(&dev));
+// Device address of the scratch array on `dev`, which must be the calling thread's current
+// device (the caller has checked that it is the index's device); looked up once per device.
+void* scratch_for_device(int dev) {
   if (dev < 0 || dev >= kMaxDevices) throw lshg::Error(LSHG_ERR_UNSUPPORTED, "device index out of range");
   std::lock_guard<std::mutex> g(g_mu);
   if (!g_scratch_ptr[dev]) {
@@ -67,6 +69,7 @@ extern "C" int lshg_index_query_noalloc(lshg_index* idx, const float* d_queries,
     if (!idx || !idx->impl || !d_results || (!d_queries && N_query > 0))
       throw Error(LSHG_ERR_INVALID_ARGUMENT, "NULL argument");
     Index& I = *idx->impl;
+    check_device(I);  // the scratch array and the index's buffers are on the same GPU
     const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
     if (I.p.framework != 0 || impl != 2 || I.dist != DIST_ANGULAR)
       throw Error(LSHG_ERR_UNSUPPORTED, "the allocation-free query serves exact angular linear-scan indexes only");
@@ -83,7 +86,7 @@ extern "C" int lshg_index_query_noalloc(lshg_index* idx, const float* d_queries,
       throw Error(LSHG_ERR_INVALID_ARGUMENT,
                   "query batch needs " + std::to_string(need) + " bytes of temporaries; the allocation-free entry "
                   "point has " + std::to_string(kNoAllocScratchBytes) + " (use fewer queries or a smaller k)");
-    unsigned char* base = static_cast<unsigned char*>(scratch_for_current_device());
+    unsigned char* base = static_cast<unsigned char*>(scratch_for_device(I.device));
     float* qnorm = reinterpret_cast<float*>(base);
     uint64_t* part = reinterpret_cast<uint64_t*>(base + qn_bytes);
     uint64_t* merged = reinterpret_cast<uint64_t*>(base + qn_bytes + part_bytes);

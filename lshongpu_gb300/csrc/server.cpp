@@ -30,6 +30,10 @@
 
 using namespace lshg;
 
+namespace lshg {
+void set_last_error(const char* msg);
+}
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -118,6 +122,7 @@ struct lshg_server {
     if (p.use_graphs && !s.no_graph[key]) {
       auto it = s.graphs.find(key);
       if (it == s.graphs.end()) {
+        idx.error_word(s.stream);  // the slot stream's error word exists before the capture
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
         bool ok = cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
@@ -303,6 +308,10 @@ int lshg_server_create(const lshg_server_params* p, lshg_server** out) {
 
 int lshg_server_add_index(lshg_server* s, int index_id, lshg_index* idx) {
   if (!s || !idx || !idx->impl) return LSHG_ERR_INVALID_ARGUMENT;
+  if (idx->impl->device != s->device) {
+    set_last_error("the index lives on another device than the server");
+    return LSHG_ERR_INVALID_ARGUMENT;
+  }
   std::lock_guard<std::mutex> g(s->mu);
   s->indexes[index_id] = idx->impl.get();
   return LSHG_OK;

@@ -512,6 +512,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   // swap near-equal neighbours at the boundary); 128 (the list kernel's maximum) beyond
   const bool e4m3 = I.p.implementation == 9;
   const int CT = k <= 32 ? 64 : 128;
+  int* err = I.error_word(s);
   const int64_t qpad = (int64_t)ceil_div(nq, BM) * BM;
   const int QT = (int)(qpad / BM);
   FilterPlan plan = plan_filter(I.n, CT);
@@ -545,10 +546,10 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, (size_t)(nq + 1) * sizeof(int), s));
   DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
   if (e4m3)
-    launch_filter_scan(ma8, mb8, mb8, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr, true,
+    launch_filter_scan(ma8, mb8, mb8, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, err, true,
                        s);
   else
-    launch_filter_scan(ma, mb256, mb256hi, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, I.qerr.ptr,
+    launch_filter_scan(ma, mb256, mb256hi, hi_cols, plan, nq, I.n, I.d, QT, CT, tau.ptr, cnt.ptr, cand.ptr, err,
                        false, s);
 
   // 3. top-CT of the survivors
@@ -563,15 +564,15 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
     launch_gather_rows(qbf.ptr, ovf, nq, qg.ptr, s);
     const CUtensorMap mg = make_map(qg.ptr, qpad);
     DevBuf<uint64_t> part((size_t)BM * (G + 2 * QT) * CT, s);
-    if (CT == 64) run_list_kernel<3, 64>(mg, mb, ovf, I.n, NT, I.d, G, part.ptr, I.qerr.ptr, s);
-    else run_list_kernel<1, 128>(mg, mb, ovf, I.n, NT, I.d, G, part.ptr, I.qerr.ptr, s);
+    if (CT == 64) run_list_kernel<3, 64>(mg, mb, ovf, I.n, NT, I.d, G, part.ptr, err, s);
+    else run_list_kernel<1, 128>(mg, mb, ovf, I.n, NT, I.d, G, part.ptr, err, s);
     launch_merge_fallback(part.ptr, ovf, nq, NT, G, CT, best.ptr, s);
   }
 
   // 5. exact FP32 re-rank with the reference's angular formula
   DevBuf<float> qn((size_t)nq, s);
   launch_row_norms(q, nq, I.d, qn.ptr, s);
-  launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s, I.qerr.ptr);
+  launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s, err);
 }
 
 }  // namespace lshg

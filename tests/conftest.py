@@ -6,7 +6,9 @@ on CPU.  The engine library and the CPU oracle are built on first use.
 from __future__ import annotations
 
 import os
+import subprocess
 import sys
+import tempfile
 
 import numpy as np
 import pytest
@@ -46,6 +48,21 @@ def golden():
         "rng": dict(np.load(os.path.join(g, "rng_streams.npz"))),
         "gold": dict(np.load(os.path.join(g, "goldstandard.npz"))),
     }
+
+
+@pytest.fixture(scope="session")
+def uniforms():
+    """cuRAND uniforms for seeds h*1234+92138 (createSeedArr, weightedMinHash.cuh:252-262),
+    from an independent test-side program; returns get(H, T) -> float32 [H][T]."""
+    src = os.path.join(ROOT, "tests", "golden", "curand_uniforms.cu")
+    exe = os.path.join(tempfile.mkdtemp(), "curand_uniforms")
+    subprocess.run(["nvcc", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe, src], check=True)
+
+    def get(H, T):
+        out = subprocess.run([exe, str(H), str(T)], capture_output=True, check=True).stdout
+        return np.frombuffer(out, np.float32).reshape(H, T)
+
+    return get
 
 
 def ids_equal_up_to_ties(ids_a, d_a, ids_b, d_b, tol):

@@ -80,3 +80,33 @@ def test_async_device_error_reported_at_sync(engine):
     assert e.value.status == 6  # LSHG_ERR_SAMPLER_LIMIT
     idx.sync()  # the error was reported once; the index stays usable
     assert idx.query(q[:3], 32).shape == (3, 32)
+
+
+def test_device_error_reported_on_its_own_stream(engine):
+    """Two streams with batches in flight on one index: only the stream whose batch holds
+    a zero query row (the weighted-MinHash sampler hits its draw limit) reports
+    LSHG_ERR_SAMPLER_LIMIT at its sync; the other stream's sync is clean and its results
+    equal the synchronous query's."""
+    import torch
+
+    x = datasets.sparse_gamma(2000, D, 153)
+    good = datasets.sparse_gamma(8, D, 154)
+    bad = good.copy()
+    bad[5] = 0.0
+    idx = engine.Index(x, implementation=4, distanceFunc=2, sketchDim=64)
+    ref = idx.query(good, 32)
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    dbad, dgood = torch.from_numpy(bad).cuda(), torch.from_numpy(good).cuda()
+    oa = torch.empty((8, 32, 2), dtype=torch.int32, device="cuda")
+    ob = torch.full((8, 32, 2), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    idx.query_device_async(dbad.data_ptr(), 8, 32, oa.data_ptr(), stream=sa.cuda_stream)
+    idx.query_device_async(dgood.data_ptr(), 8, 32, ob.data_ptr(), stream=sb.cuda_stream)
+    idx.sync(sb.cuda_stream)  # clean: stream A's error is not reported here
+    with pytest.raises(engine.LshgError) as e:
+        idx.sync(sa.cuda_stream)
+    assert e.value.status == 6  # LSHG_ERR_SAMPLER_LIMIT
+    idx.sync(sa.cuda_stream)  # reported once
+    got = ob.cpu().numpy()
+    assert np.array_equal(got[:, :, 0], ref["ID"])
+    assert np.array_equal(got[:, :, 1].view(np.float32), ref["distance"])

@@ -5,10 +5,6 @@ compared bit-exactly where the reference's arithmetic is restated exactly (angul
 generalized Jaccard, Hamming/Jaccard sketch distances, JL projections) and with a
 stated tolerance for the Euclidean distance (the reference squares through pow()).
 """
-import os
-import subprocess
-import tempfile
-
 import numpy as np
 import pytest
 
@@ -21,21 +17,6 @@ D = 100
 
 def data(n, nq, seed=5, d=D):
     return datasets.clustered(n, d, seed, count=20), datasets.clustered(nq, d, seed + 1, count=20)
-
-
-@pytest.fixture(scope="module")
-def uniforms():
-    """cuRAND uniforms for seeds h*1234+92138, from an independent test-side program."""
-    src = os.path.join(os.path.dirname(__file__), "golden", "curand_uniforms.cu")
-    tmp = tempfile.mkdtemp()
-    exe = os.path.join(tmp, "curand_uniforms")
-    subprocess.run(["nvcc", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe, src], check=True)
-
-    def get(H, T):
-        out = subprocess.run([exe, str(H), str(T)], capture_output=True, check=True).stdout
-        return np.frombuffer(out, np.float32).reshape(H, T)
-
-    return get
 
 
 # ---- implementation 2: exact scan -----------------------------------------------------

@@ -178,3 +178,79 @@ def test_lsh_bad_key_range_rejected(engine):
     x, q = data(100, 2)
     with pytest.raises(engine.LshgError):
         engine.LSH(2, 7, 32, D, 2, 100, x, q, 0, 1, 6, 4, False)  # 2P = 256 keys > 2^6 buckets
+
+
+# ---- weighted-MinHash bucket keys (keysImplementation 4 and 5) ---------------------------
+
+def wmh_keys_oracle(orc, xs, start, mp, M, u, H, onebit, tables, bits, bm):
+    """Keys of shifted, normalised rows: byte samples (one per table, u8 widened to u16)
+    or `bits` one-bit samples packed into a word per table (lshFramework.cuh:47-53 ->
+    weightedMinHash.cuh:432-466)."""
+    sk, over = orc.wmh_sketch(xs, start, mp, M, u, H, u.shape[1], onebit, tables, bits, bm)
+    assert over == 0
+    return (sk & 0xFFFF).astype(np.uint16) if onebit else sk.astype(np.uint16)
+
+
+def shift_by_base(x, q):
+    """The recorded min shift replayed on queries: |min floor| over the base only."""
+    mn = np.minimum(0, np.floor(x).min(axis=0)).astype(np.int32)
+    return (np.asarray(q, np.float32) + np.abs(mn).astype(np.float32)).astype(np.float32)
+
+
+@pytest.mark.parametrize("onebit,bits,dist", [(0, 8, 2), (0, 10, 1), (1, 6, 1), (1, 12, 2)])
+def test_wmh_keys_buckets_query(engine, orc, uniforms, onebit, bits, dist):
+    """Weighted-MinHash keys: byte samples (keysImplementation 4) and one-bit samples
+    (5) at two bucketKeyBits each.  Index (statistics from the base): base and query keys
+    bit-exact, bucket offsets and contents equal to the oracle's, query results equal.
+    Reference entry point LSH() (statistics over base and queries, as runLsh computes
+    them): results equal to the oracle's."""
+    n, nq, L = 3000, 12, 6
+    x = datasets.sparse_gamma(n, D, 91 + bits)
+    q = datasets.sparse_gamma(nq, D, 191 + bits)
+    keys_impl = 5 if onebit else 4
+    H = L * bits if onebit else L
+    S = 1 << bits
+    u = uniforms(H, 4096)
+    bm = orc.random_bools(255)
+
+    # resident index: shift and normalise with the base's statistics, replayed on queries
+    idx = engine.Index(x, implementation=2, distanceFunc=dist, framework=1, keysImplementation=keys_impl,
+                       bucketKeyBits=bits, tables=L)
+    xs, _ = orc.jaccard_shift(x, x[:0])
+    xs = orc.normalize(xs)
+    qs = orc.normalize(shift_by_base(x, q))
+    start, mp, M = orc.wmh_bounds(xs, xs[:0])
+    okeys = wmh_keys_oracle(orc, xs, start, mp, M, u, H, onebit, L, bits, bm)
+    if not onebit:
+        assert okeys.max() < S
+    keys, off, bk = lsh_index_arrays(engine, idx, n, L, S)
+    assert np.array_equal(keys, okeys)
+    ooff, obk = orc.lsh_build(okeys, L, S)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(bk, obk)
+    oqk = wmh_keys_oracle(orc, qs, start, mp, M, u, H, onebit, L, bits, bm)
+    _, qk = idx.sketch_queries(q, np.uint32, 0, L)
+    assert np.array_equal(qk, oqk)
+    res = idx.query(q, 32)
+    ids, ds = orc.lsh_query(xs, qs, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, dist, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
+    assert (ids[:, 0] >= 0).all()  # every query finds candidates in its buckets
+
+    # reference entry point: statistics over base and queries
+    r = engine.LSH(2, keys_impl, 32, D, nq, n, x, q, 0, dist, bits, L, False)
+    xs2, qs2 = orc.jaccard_shift(x, q)
+    xs2, qs2 = orc.normalize(xs2), orc.normalize(qs2)
+    start2, mp2, M2 = orc.wmh_bounds(xs2, qs2)
+    ok2 = wmh_keys_oracle(orc, xs2, start2, mp2, M2, u, H, onebit, L, bits, bm)
+    oq2 = wmh_keys_oracle(orc, qs2, start2, mp2, M2, u, H, onebit, L, bits, bm)
+    off2, bk2 = orc.lsh_build(ok2, L, S)
+    ids2, ds2 = orc.lsh_query(xs2, qs2, oq2, L, S, off2, bk2, 0, 0, None, None, 0, 32, dist, 32)
+    assert np.array_equal(r.ids, ids2)
+    assert np.array_equal(r.distances, ds2)
+
+
+def test_wmh_byte_keys_need_256_buckets(engine):
+    x = datasets.sparse_gamma(200, D, 5)
+    with pytest.raises(engine.LshgError):
+        engine.Index(x, implementation=2, distanceFunc=2, framework=1, keysImplementation=4, bucketKeyBits=7, tables=4)

@@ -91,6 +91,36 @@ def test_reference_minhash_samples(engine, onebit):
     assert np.array_equal(mine, ref)
 
 
+@pytest.mark.parametrize("onebit,bits", [(0, 8), (1, 10)])
+def test_reference_minhash_keys(engine, onebit, bits):
+    """LSH bucket keys from weighted MinHash (keysImplementation 4 / 5): the reference
+    runs its sampler in key mode (lshFramework.cuh:47-53 -> weightedMinHash.cuh:432-466,
+    sketchedDim = tables, hashBits = bucketKeyBits); the engine's exported keys must equal
+    the reference kernel's samples on the engine's preprocessed base."""
+    import subprocess
+    import tempfile
+    import os
+
+    n, L = 1500, 6
+    x = datasets.sparse_gamma(n, D, 107 + bits)
+    idx = engine.Index(x, implementation=2, distanceFunc=2, framework=1, keysImplementation=5 if onebit else 4,
+                       bucketKeyBits=bits, tables=L)
+    xp = np.frombuffer(idx.export(engine.EXPORT_DATA), np.float32).reshape(n, D)
+    start, mp, M = oracle.wmh_bounds(xp, xp[:0])
+    H = L * bits if onebit else L
+    src = os.path.join(os.path.dirname(__file__), "golden", "curand_uniforms.cu")
+    exe = os.path.join(tempfile.mkdtemp(), "cu")
+    subprocess.run(["nvcc", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-o", exe, src], check=True)
+    u = np.frombuffer(subprocess.run([exe, str(H), "4096"], capture_output=True, check=True).stdout,
+                      np.float32).reshape(H, 4096)
+    bm = engine.random_bools(255)
+    _, over = oracle.wmh_sketch(xp, start, mp, M, u, H, 4096, onebit, L, bits, bm)
+    assert over == 0  # every sample ends within 4096 draws before the reference kernel runs
+    ref = oracle.ref_wmh(xp, start, mp, M, H, onebit, L, bits, bm)
+    mine = np.frombuffer(idx.export(engine.EXPORT_KEYS), np.uint16).reshape(n, L)
+    assert np.array_equal(mine, ref.astype(np.uint16))
+
+
 def test_reference_exact_scan_config1_timing(engine):
     """Plain exact angular scan on config 1 (N=100,000 x 100, Q=1,000, k=32): the
     reference kernel and the engine's SIMT and tensor-core scans on the same GPU.

@@ -80,3 +80,54 @@ def test_persistence_roundtrip(engine, indexes):
                 f.write(bytes([b[0] ^ 0xFF]))
             with pytest.raises(engine.LshgError):
                 engine.Index.load(p)
+
+
+def _with_checksum(buf: bytearray) -> bytearray:
+    """Recompute the file's trailing FNV-1a 64 checksum after an edit."""
+    h = 1469598103934665603
+    for c in bytes(buf[:-8]):
+        h = ((h ^ c) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    buf[-8:] = h.to_bytes(8, "little")
+    return buf
+
+
+def test_load_rejects_inconsistent_files(engine):
+    """A file whose checksum is valid but whose scalars disagree with its buffers (or
+    that names an unknown implementation) is refused with LSHG_ERR_IO before any of it
+    reaches the GPU; a truncated file is refused too; the intact file still loads."""
+    import ctypes as C
+
+    from lshongpu_gb300._lib import IndexParams
+
+    x = datasets.clustered(300, 16, 5, count=10)
+    q = datasets.clustered(8, 16, 6, count=10)
+    ix = engine.Index(x, implementation=2, distanceFunc=1)
+    off_params, off_n = 8, 8 + C.sizeof(IndexParams)
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "ix.lshg")
+        ix.save(p)
+        good = bytearray(open(p, "rb").read())
+
+        def n_plus_one(b):
+            b[off_n:off_n + 8] = (301).to_bytes(8, "little")
+
+        def unknown_impl(b):
+            b[off_params:off_params + 4] = (7).to_bytes(4, "little")
+
+        for edit in (n_plus_one, unknown_impl):
+            b = bytearray(good)
+            edit(b)
+            with open(p, "wb") as f:
+                f.write(_with_checksum(b))
+            with pytest.raises(engine.LshgError) as e:
+                engine.Index.load(p)
+            assert e.value.status == 9
+            assert "inconsistent" in str(e.value)
+        with open(p, "wb") as f:
+            f.write(good[: len(good) // 2])
+        with pytest.raises(engine.LshgError) as e:
+            engine.Index.load(p)
+        assert e.value.status == 9
+        with open(p, "wb") as f:
+            f.write(good)
+        assert np.array_equal(engine.Index.load(p).query(q, 32), ix.query(q, 32))

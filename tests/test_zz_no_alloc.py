@@ -24,9 +24,13 @@ def test_noalloc_matches_allocating_entry_point(engine):
     x = datasets.clustered(20000, D, 81, count=40)
     q1 = datasets.clustered(300, D, 82, count=40)
     q2 = datasets.clustered(300, D, 83, count=40)
+    q3 = datasets.clustered(200, D, 84, count=40)
+    q4 = datasets.clustered(48, D, 85, count=40)
     idx = engine.Index(x, implementation=engine.IMPL_EXACT, distanceFunc=engine.ANGULAR)
     lib = engine.lib()
-    for q, k in ((q1, 32), (q2, 100)):
+    # k <= 128 runs the register-blocked scan; k = 256 and 1024 the general scan with
+    # block top-C queues and a merge of the per-split lists
+    for q, k in ((q1, 32), (q2, 100), (q3, 256), (q4, 1024)):
         dq = torch.from_numpy(q).cuda()
         ref = torch.empty((q.shape[0], k, 2), dtype=torch.int32, device="cuda")
         idx.query_device(dq.data_ptr(), q.shape[0], k, ref.data_ptr())
