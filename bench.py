@@ -197,6 +197,21 @@ def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
             (entries * 4 + distinct * (4 * dims + 4) + nq * (4 * dims + 8 * K)) / 1e9, "GB/s")
 
 
+def dram_traffic(kernel: str, workload: str):
+    """DRAM bytes (read + write) of one launch of `kernel` on `workload`, as an ncu capture
+    of the same kernel and workload measured them (profiles/dram_traffic.json, which names
+    the capture's command); None where no capture of that pair exists."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            rows = json.load(f)["captures"]
+    except Exception:
+        return None
+    for r in rows:
+        if r["kernel"] == kernel and r["workload"] == workload:
+            return r["dram_bytes_per_launch"]
+    return None
+
+
 def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7) -> dict:
     """Open-loop Poisson arrivals of requests (batch size log-uniform in [1, 4096], k from
     {10, 32, 100}, index type drawn uniformly) against the continuous-batching server;
@@ -265,6 +280,24 @@ def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7
             "graph_replays": st["graph_replays"] - st0["graph_replays"], "rejected": st["rejected"] - st0["rejected"]}
 
 
+def fp64_distances(x, q, ids, dist_fn):
+    """Double-precision distance of every (query, returned id): angular 1 - cos, or
+    generalized Jaccard 1 - sum(min)/sum(max) on the shifted, normalised rows."""
+    if dist_fn == 2:
+        xs = x.astype(np.float64)
+        qs = q.astype(np.float64)
+        sh = np.abs(np.minimum(0, np.floor(np.minimum(xs.min(axis=0), qs.min(axis=0)))))
+        xs, qs = xs + sh, qs + sh
+        xs /= np.linalg.norm(xs, axis=1, keepdims=True)
+        qs /= np.linalg.norm(qs, axis=1, keepdims=True)
+        rows = xs[ids]
+        return 1.0 - np.minimum(rows, qs[:, None, :]).sum(-1) / np.maximum(rows, qs[:, None, :]).sum(-1)
+    qq = q.astype(np.float64)
+    rows = x[ids].astype(np.float64)
+    dot = np.einsum("qd,qkd->qk", qq, rows)
+    return 1.0 - dot / (np.linalg.norm(qq, axis=1)[:, None] * np.linalg.norm(rows, axis=2))
+
+
 def workload_text(args) -> str:
     d = f"{DIM}" if not PAD_DIM else f"{DIM + PAD_DIM} ({DIM} + {PAD_DIM} zero dims)"
     data = ("sparse Gamma(2,1) values, 30% nonzero" if DATA == "sparse"
@@ -299,11 +332,16 @@ def run_reference_arm(args, world, rank):
     line = {
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_q * N_QUERY * 1e3,
+        "ms_per_step_kind": f"extrapolated: the measured time of a {sample}-query sample scaled to the {N_QUERY}-query "
+                            f"batch",
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"exact angular k-NN, N={N_BASE}, d={DIM}, Q={N_QUERY} (timed on a {sample}-query "
                                f"sample per step), k={K}", "global_batch": N_QUERY, "l2": "inputs larger than L2"},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} queries x {N_BASE} points per step, {args.steps} steps"},
+                         "sample": f"{sample} queries x {N_BASE} points per step, {args.steps} steps",
+                         "note": "port of GoldStandard/goldstandard.cpp computeGoldStandard (same arithmetic: float "
+                                 "magnitudes, double-accumulated dot, full sort), run on all host threads without the "
+                                 "reference's per-point struct copies: faster than the single-threaded reference"},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -466,10 +504,7 @@ def main():
         peak, peak_kind = POPC_NOMINAL_GWORDS, "nominal (152 SMs x 16 popc/clk x 2.07 GHz)"
     else:
         peak = None
-    # DRAM bytes of one tc_filter launch at the headline shape, from the committed ncu
-    # capture (profiles/tc_filter_1.2Mx100_q10k_dram.md): the base once + survivors
-    traffic = 310.19e6 + 36.78e6 if (args.config is None and args.path == "tc" and N_BASE == 1_200_000
-                                     and N_QUERY == 10_000) else None
+    traffic = dram_traffic(kname, workload_text(args))
     roofline = {"bound": bound, "kernel": kname, "achieved": achieved, "peak": peak, "unit": unit,
                 "frac": (achieved / peak) if (achieved and peak) else None, "peak_source": peak_kind,
                 "traffic": traffic, "traffic_unit": "bytes per launch" if traffic else None, "kernel_ms_per_launch": (kms / cnt) if cnt else None,
@@ -496,17 +531,32 @@ def main():
         import oracle
 
         threads = os.cpu_count() or 1
-        res = out.cpu().numpy().view(np.int32)[:, :, 0]
+        got = out.cpu().numpy()
+        res = got[:, :, 0]
         headline = args.config is None and args.path == "tc"
+        dist_fn = 2 if DATA == "sparse" else 1
         if DATA == "sparse":  # generalized-Jaccard truth (single-threaded oracle: small sample)
             nchk = 50
-            tids, _ = oracle.exact_topk(x, q[:nchk], K, dist=2)
+            tids, tds = oracle.exact_topk(x, q[:nchk], K, dist=2)
         else:
             nchk = 200
-            tids, _ = oracle.fp64_topk(x, q[:nchk], K, threads=threads)
+            tids, tds = oracle.fp64_topk(x, q[:nchk], K, threads=threads)
         rec = np.mean([len(set(res[i].tolist()) & set(tids[i].tolist())) / K for i in range(nchk)])
         extras["recall_at_32"] = float(rec)
         extras["recall_queries"] = nchk
+        # distance error of the returned points against their FP64 distances, and the
+        # reference's distance ratio (validation.cpp:160-198: sum of returned distances over
+        # sum of the truth's, averaged over queries)
+        rid = res[:nchk]
+        rd32 = got[:nchk, :, 1].view(np.float32).astype(np.float64)
+        ok = rid >= 0
+        d64 = fp64_distances(x, q[:nchk], np.where(ok, rid, 0), dist_fn)
+        extras["max_dist_err_vs_fp64"] = float(np.max(np.abs(rd32 - d64)[ok])) if ok.any() else None
+        truth = np.zeros((nchk, K), dtype=L.POINT_DTYPE)
+        truth["ID"], truth["distance"] = tids, np.asarray(tds, np.float64).astype(np.float32)
+        _, ratio = L.validate(truth, np.ascontiguousarray(got[:nchk]).view(L.POINT_DTYPE).reshape(nchk, K), K)
+        extras["distance_ratio"] = float(ratio)
+        extras["truth"] = "FP64 oracle" if DATA != "sparse" else "FP32 generalized-Jaccard oracle"
         # CPU baseline: GoldStandard port, bounded sample, all host threads
         if DATA != "sparse":
             sample = 2 * threads

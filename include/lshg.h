@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define LSHG_ABI_VERSION 1
+#define LSHG_ABI_VERSION 2
 
 typedef enum {
   LSHG_OK = 0,
@@ -82,6 +82,13 @@ typedef struct lshg_options_s {
   int cp_hashes;         /* cross-polytope hashes concatenated per table key (reference: 1) */
   int cp_rounds;         /* cross-polytope rotation rounds (reference: 3, crossPolyTope.cuh:44) */
   void* stream;          /* cudaStream_t to run on, NULL = a library-owned stream */
+  int fp64_recheck;      /* re-score, in double precision on the GPU, the re-ranked candidates
+                            whose FP32 distance lies within the FP32 error bound of the k-th
+                            one, and order those by the FP64 distance (ties: lower index);
+                            returned distances stay FP32.  -1 (default) = on for the
+                            tensor-core scans (8, 9), off elsewhere; 0 = off; 1 = on for every
+                            re-ranked scan (3-6, 8, 9).  The exact scan (2) returns the
+                            reference's FP32 order. */
 } lshg_options;
 
 /* ---- library ---------------------------------------------------------------------- */

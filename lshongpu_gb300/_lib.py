@@ -41,6 +41,7 @@ class Options(C.Structure):
         ("cp_hashes", c_int),
         ("cp_rounds", c_int),
         ("stream", c_void_p),
+        ("fp64_recheck", c_int),
     ]
 
 

@@ -93,7 +93,7 @@ class Result:
 
 
 def make_options(thread_queue_size: int = 128, candidates: int = 0, cp_hashes: int = 1, cp_rounds: int = 3,
-                 stream: int | None = None) -> Options:
+                 stream: int | None = None, fp64_recheck: int = -1) -> Options:
     o = Options()
     lib().lshg_options_default(C.byref(o))
     o.thread_queue_size = thread_queue_size
@@ -101,6 +101,7 @@ def make_options(thread_queue_size: int = 128, candidates: int = 0, cp_hashes: i
     o.cp_hashes = cp_hashes
     o.cp_rounds = cp_rounds
     o.stream = stream
+    o.fp64_recheck = fp64_recheck
     return o
 
 

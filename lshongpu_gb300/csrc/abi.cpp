@@ -155,6 +155,7 @@ void lshg_options_default(lshg_options* opt) {
   opt->cp_hashes = 1;
   opt->cp_rounds = 3;
   opt->stream = nullptr;
+  opt->fp64_recheck = -1;
 }
 
 int lshg_linear_scans_ex(int implementation, int k, int d, int N_query, int N_data, const float* data,

@@ -579,7 +579,8 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     launch_merge_splits(part.ptr, nq, splits, C, merged.ptr, s);
     cand = merged.ptr;
   }
-  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s));
+  launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
+                I.p.opt.fp64_recheck > 0);
 }
 
 }  // namespace lshg

@@ -85,10 +85,14 @@ int scan_bits_splits(int64_t n, int nq, int C);
 // ---- rerank.cu -------------------------------------------------------------------
 // Merge per-split sorted lists into one sorted list of C keys per query.
 void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
-// Exact re-rank of candidate keys (candidateSetScanner.cuh:10-32) and top-k output.
+// Exact re-rank of candidate keys (candidateSetScanner.cuh:10-32) and top-k output;
+// fp64_recheck: re-score the candidates within the FP32 error bound of the k-th distance
+// in double precision and order those by the FP64 distance.
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d,
                    const float* xnorm, const float* q, const float* qnorm, int dist, int k,
-                   struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr);
+                   struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr, bool fp64_recheck = false);
+// The FP64 band of the re-rank: |FP32 distance - k-th| <= band_abs + band_rel * |k-th|.
+void fp64_band(int dist, int d, float* band_abs, float* band_rel);
 // Keys to result points (ID, distance); empty keys become (-1, INT_MAX).
 void launch_keys_to_points(const uint64_t* keys, int nq, int C, int k, struct ::lshg_point_s* out,
                            cudaStream_t s);

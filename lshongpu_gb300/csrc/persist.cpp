@@ -22,7 +22,7 @@ void set_last_error(const char* msg);
 
 namespace {
 
-constexpr char kMagic[8] = {'L', 'S', 'H', 'G', 'I', 'D', 'X', '2'};
+constexpr char kMagic[8] = {'L', 'S', 'H', 'G', 'I', 'D', 'X', '3'};
 
 struct Writer {
   FILE* f;

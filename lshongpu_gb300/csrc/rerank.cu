@@ -6,6 +6,12 @@
 // (distance, id) and the first k written in ascending order -- the order the reference
 // produces by writing its sorted warp queue back to front (sketchedDistanceScanners.cuh:
 // 84-99).  Empty candidates (no point) become (-1, INT_MAX) as in the reference.
+//
+// FP64 boundary re-check (optional, on by default for the tensor-core scans): after the
+// FP32 sort, the candidates whose FP32 distance lies within the FP32 error bound of the
+// k-th one are re-scored in double precision and reordered by (FP64 distance, id), so the
+// top-k set and its order at the boundary are those of the exact distances.  Returned
+// distances stay the FP32 values of the reference's formula.
 #include "common.cuh"
 #include "kernels.h"
 #include "launch_count.h"
@@ -17,6 +23,99 @@
 namespace lshg {
 
 namespace {
+
+constexpr int kBandMax = 256;  // entries a query's FP64 band re-scores at most
+
+// Double-precision distance of float rows, same definition as the FP32 formula: products
+// rounded, then added in dimension order (no fused multiply-add), as the FP64 CPU oracle.
+template <int DIST>
+__device__ double fp64_distance(const float* __restrict__ xr, const float* qr, int d) {
+  if (DIST == DIST_ANGULAR) {
+    double dot = 0.0, qq = 0.0, xx = 0.0;
+    for (int j = 0; j < d; ++j) {
+      const double a = qr[j], b = xr[j];
+      dot = __dadd_rn(dot, __dmul_rn(a, b));
+      qq = __dadd_rn(qq, __dmul_rn(a, a));
+      xx = __dadd_rn(xx, __dmul_rn(b, b));
+    }
+    return __dadd_rn(1.0, -__ddiv_rn(dot, __dmul_rn(__dsqrt_rn(qq), __dsqrt_rn(xx))));
+  } else if (DIST == DIST_JACCARD) {
+    double mn = 0.0, mx = 0.0;
+    for (int j = 0; j < d; ++j) {
+      const double a = xr[j], b = qr[j];
+      mn = __dadd_rn(mn, fmin(a, b));
+      mx = __dadd_rn(mx, fmax(a, b));
+    }
+    return __dadd_rn(1.0, -__ddiv_rn(mn, mx));
+  } else {
+    double acc = 0.0;
+    for (int j = 0; j < d; ++j) {
+      const double df = __dadd_rn((double)qr[j], -(double)xr[j]);
+      acc = __dadd_rn(acc, __dmul_rn(df, df));
+    }
+    return DIST == DIST_EUCLID ? __dsqrt_rn(acc) : acc;
+  }
+}
+
+__device__ __forceinline__ uint64_t double_to_ordered(double v) {
+  const uint64_t u = (uint64_t)__double_as_longlong(v == 0.0 ? 0.0 : v);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// Reorders keys[lo..hi] (sorted by FP32 key) by FP64 distance, where [lo, hi] holds every
+// candidate whose FP32 distance is within band_abs + band_rel * |kth| of the k-th one.
+// Called by every thread of the block after the sort; qr is the query row.
+template <int DIST>
+__device__ void fp64_boundary(uint64_t* keys, int C, int k, const float* __restrict__ x, int d, const float* qr,
+                              float band_abs, float band_rel) {
+  __shared__ int s_lo, s_hi;
+  __shared__ uint64_t s_ord[kBandMax];
+  __shared__ uint64_t s_key[kBandMax];
+  const int kk = imin(k, C) - 1;
+  const uint64_t kth_key = keys[kk];
+  if (kth_key == kEmptyKey) return;  // fewer than k candidates: no boundary (block-uniform)
+  const float kth = key_dist(kth_key);
+  const float band = band_abs + band_rel * fabsf(kth);
+  if (threadIdx.x == 0) {
+    s_lo = kk;
+    s_hi = kk;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < C; i += blockDim.x) {
+    const uint64_t key = keys[i];
+    if (key != kEmptyKey && fabsf(key_dist(key) - kth) <= band) {
+      atomicMin(&s_lo, i);
+      atomicMax(&s_hi, i);
+    }
+  }
+  __syncthreads();
+  int lo = s_lo, hi = s_hi;
+  if (hi - lo + 1 > kBandMax) {  // massive near-ties: the kBandMax entries around the k-th
+    lo = imax(lo, kk - (kBandMax / 2 - 1));
+    hi = imin(hi, lo + kBandMax - 1);
+    lo = imax(s_lo, hi - kBandMax + 1);
+  }
+  const int m = hi - lo + 1;
+  if (m < 2) return;  // block-uniform
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const uint64_t key = keys[lo + t];
+    s_key[t] = key;
+    s_ord[t] = double_to_ordered(fp64_distance<DIST>(x + (int64_t)key_id(key) * d, qr, d));
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const uint64_t ot = s_ord[t];
+    const uint32_t it = (uint32_t)key_id(s_key[t]);
+    int r = 0;
+    for (int j = 0; j < m; ++j) {
+      const uint64_t oj = s_ord[j];
+      const uint32_t ij = (uint32_t)key_id(s_key[j]);
+      r += (oj < ot) || (oj == ot && (ij < it || (ij == it && j < t)));
+    }
+    keys[lo + r] = s_key[t];
+  }
+  __syncthreads();
+}
 
 // One block per query: fold S sorted lists of C keys into one.
 __global__ void merge_splits_kernel(const uint64_t* __restrict__ in, int nq, int splits, int C,
@@ -41,7 +140,8 @@ __global__ void merge_splits_kernel(const uint64_t* __restrict__ in, int nq, int
 template <int DIST>
 __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                               int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
-                              const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out) {
+                              const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, float band_abs,
+                              float band_rel) {
   extern __shared__ __align__(16) unsigned char rsm[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(rsm);
   float* qr = reinterpret_cast<float*>(rsm + (size_t)C * 8);
@@ -63,6 +163,7 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
+  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, d, qr, band_abs, band_rel);
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -80,7 +181,8 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
 template <int DIST>
 __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                                      int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
-                                     const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, int* err) {
+                                     const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, int* err,
+                                     float band_abs, float band_rel) {
   extern __shared__ __align__(128) unsigned char rsm[];
   const int CH = blockDim.x;
   const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
@@ -142,6 +244,7 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
+  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, d, qr, band_abs, band_rel);
   for (int i = tid; i < k; i += CH) {
     const uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -182,9 +285,27 @@ void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t
   LSHG_CHECK_LAUNCH();
 }
 
+void fp64_band(int dist, int d, float* band_abs, float* band_rel) {
+  // Twice the bound E on |FP32 distance - exact distance| (u = 2^-24, d-term sequential
+  // sums: relative error <= d*u each): a candidate outside [kth - 2E, kth + 2E] is on the
+  // same side of the k-th in FP32 and in exact arithmetic.  Angular: the dot within d*u of
+  // |q||x|, each norm within (d/2 + 1)*u, product and quotient 2u, the subtraction u:
+  // E <= (2d + 7)u.  Jaccard: two sums within d*u, quotient and subtraction: E <= (2d + 3)u.
+  // Euclidean: relative, E <= (d + 3)u |distance|.
+  const double u = 1.0 / 16777216.0;
+  *band_abs = 0.0f;
+  *band_rel = 0.0f;
+  if (dist == DIST_ANGULAR) *band_abs = (float)(2.0 * (2.0 * d + 7.0) * u);
+  else if (dist == DIST_JACCARD) *band_abs = (float)(2.0 * (2.0 * d + 3.0) * u);
+  else *band_rel = (float)(2.0 * (d + 3.0) * u);
+}
+
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d, const float* xnorm,
-                   const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s, int* err) {
+                   const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s, int* err,
+                   bool fp64_recheck) {
   if (nq <= 0) return;
+  float band_abs = -1.0f, band_rel = 0.0f;
+  if (fp64_recheck) fp64_band(dist, d, &band_abs, &band_rel);
   LSHG_REQUIRE((C & (C - 1)) == 0 && C >= 2, "re-rank: candidate count must be a power of two");
   ProfScope _ps("rerank", s);
   // staged: rows of d % 4 == 0 floats, 16-byte aligned, up to 128 a chunk
@@ -195,7 +316,8 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
   do {                                                                                                         \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_staged_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                    (int)staged_smem));                                                         \
-    rerank_staged_kernel<DV><<<nq, CH, staged_smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, err); \
+    rerank_staged_kernel<DV><<<nq, CH, staged_smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, err, \
+                                                         band_abs, band_rel);                                \
   } while (0)
     switch (dist) {
       case DIST_ANGULAR: LSHG_RRS(DIST_ANGULAR); break;
@@ -215,7 +337,8 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
 #define LSHG_RR(DV)                                                                                       \
   do {                                                                                                    \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-    rerank_kernel<DV><<<nq, threads, smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out);           \
+    rerank_kernel<DV><<<nq, threads, smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, band_abs,   \
+                                                band_rel);                                                \
   } while (0)
   switch (dist) {
     case DIST_ANGULAR: LSHG_RR(DIST_ANGULAR); break;

@@ -572,7 +572,8 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   // 5. exact FP32 re-rank with the reference's angular formula
   DevBuf<float> qn((size_t)nq, s);
   launch_row_norms(q, nq, I.d, qn.ptr, s);
-  launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s, err);
+  launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s, err,
+                I.p.opt.fp64_recheck != 0);
 }
 
 }  // namespace lshg

@@ -180,3 +180,56 @@ def test_tc_fp8_overflow_and_persistence(engine, orc, tmp_path):
     idx.save(p)
     again = engine.Index.load(p).query(q, 32)
     assert np.array_equal(again, res)
+
+
+def near_tie_set(nq=16, close=24, ties=20, background=20000, seed=7):
+    """Per query: `close` points well inside its top-k, then `ties` copies of one point at
+    cosine distance ~0.2 whose coordinates differ by single-ulp nudges, so their exact
+    distances differ by ~1e-9 -- below FP32 resolution at 0.2 (ulp 1.5e-8) -- and the
+    k-th boundary falls among them; plus random background points far away."""
+    g = np.random.default_rng(seed)
+    q = g.standard_normal((nq, D))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+
+    def toward(qv, cos):
+        r = g.standard_normal(D)
+        r -= r.dot(qv) * qv
+        r /= np.linalg.norm(r)
+        return cos * qv + np.sqrt(1 - cos * cos) * r
+
+    rows = [g.standard_normal((background, D))]
+    for qv in q:
+        rows.append(np.array([toward(qv, 0.995 - 0.001 * c) for c in range(close)]))
+        p0 = toward(qv, 0.8).astype(np.float32)
+        tie = np.repeat(p0[None], ties, axis=0)
+        for t in range(ties):
+            for j in g.choice(D, 6, replace=False):
+                tie[t, j] = np.nextafter(tie[t, j], np.float32(np.inf if g.random() < 0.5 else -np.inf))
+        rows.append(tie)
+    x = np.concatenate(rows).astype(np.float32)
+    x = x[g.permutation(len(x))]
+    return np.ascontiguousarray(x), q.astype(np.float32)
+
+
+@pytest.mark.parametrize("impl", [8, 9])
+def test_fp64_boundary_recheck_orders_near_ties(engine, orc, impl):
+    """With the FP64 boundary re-check (default for implementations 8 and 9) the top-k ids
+    and their order equal the FP64 oracle's on a set built so that FP32 and FP64 orders
+    differ at the k-th place; without it (fp64_recheck = 0) they differ on most queries.
+    Returned distances are the FP32 distances of the reference's formula, within the
+    FP32 error bound (2d + 7) * 2^-24 of the FP64 distance."""
+    k = 32
+    x, q = near_tie_set()
+    ids64, d64 = orc.fp64_topk(x, q, k)
+    on = engine.Index(x, implementation=impl, distanceFunc=1).query(q, k)
+    off = engine.Index(x, implementation=impl, distanceFunc=1,
+                       options=engine.make_options(fp64_recheck=0)).query(q, k)
+    assert np.array_equal(on["ID"], ids64)
+    assert (~np.all(off["ID"] == ids64, axis=1)).sum() >= len(q) // 2  # the case this test is for
+    ids32, ds32 = orc.exact_topk(x, q, 64, dist=1)
+    bound = (2 * D + 7) * 2.0 ** -24
+    for qi in range(len(q)):
+        exact = dict(zip(ids32[qi].tolist(), ds32[qi].tolist()))
+        for pid, dist, dd in zip(on["ID"][qi].tolist(), on["distance"][qi].tolist(), d64[qi]):
+            assert np.float32(dist) == np.float32(exact[pid])
+            assert abs(dist - dd) <= bound
