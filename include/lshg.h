@@ -83,12 +83,19 @@ typedef struct lshg_options_s {
   int cp_rounds;         /* cross-polytope rotation rounds (reference: 3, crossPolyTope.cuh:44) */
   void* stream;          /* cudaStream_t to run on, NULL = a library-owned stream */
   int fp64_recheck;      /* re-score, in double precision on the GPU, the re-ranked candidates
-                            whose FP32 distance lies within the FP32 error bound of the k-th
-                            one, and order those by the FP64 distance (ties: lower index);
-                            returned distances stay FP32.  -1 (default) = on for the
+                            whose FP32 distance lies within the FP32 error bound of a
+                            neighbour's (at the k-th place or anywhere among the first 256),
+                            and order those by the FP64 distance (ties: lower index); so the
+                            top-k is the FP64 top-k of the candidates for every k.  Returned
+                            distances stay FP32.  -1 (default) = on for the
                             tensor-core scans (8, 9), off elsewhere; 0 = off; 1 = on for every
                             re-ranked scan (3-6, 8, 9).  The exact scan (2) returns the
                             reference's FP32 order. */
+  int sketch_scan;       /* Hamming / one-bit Jaccard sketch scans (3, 5) with rows of at most
+                            1024 bits: 0 (default) = tensor cores for batches of 64 queries or
+                            more, XOR/popcount otherwise; 1 = always XOR/popcount (and no E4M3
+                            copy of the sketches is kept); 2 = tensor cores whenever the base
+                            allows.  Both give the same candidates (ties: lower index). */
 } lshg_options;
 
 /* ---- library ---------------------------------------------------------------------- */

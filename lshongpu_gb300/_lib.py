@@ -42,6 +42,7 @@ class Options(C.Structure):
         ("cp_rounds", c_int),
         ("stream", c_void_p),
         ("fp64_recheck", c_int),
+        ("sketch_scan", c_int),
     ]
 
 

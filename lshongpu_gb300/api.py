@@ -35,6 +35,8 @@ KEYS_SIMHASH = 3
 KEYS_WMH = 4
 KEYS_WMH_ONEBIT = 5
 KEYS_CROSSPOLY = 7
+# sketch_scan option: how Hamming / one-bit Jaccard sketch scans run
+SKETCH_SCAN_AUTO, SKETCH_SCAN_POPCOUNT, SKETCH_SCAN_TENSOR = 0, 1, 2
 # distance functions (distanceFunctions.cuh:54-71)
 ANGULAR, JACCARD, EUCLIDEAN = 1, 2, 3
 
@@ -93,7 +95,7 @@ class Result:
 
 
 def make_options(thread_queue_size: int = 128, candidates: int = 0, cp_hashes: int = 1, cp_rounds: int = 3,
-                 stream: int | None = None, fp64_recheck: int = -1) -> Options:
+                 stream: int | None = None, fp64_recheck: int = -1, sketch_scan: int = 0) -> Options:
     o = Options()
     lib().lshg_options_default(C.byref(o))
     o.thread_queue_size = thread_queue_size
@@ -102,6 +104,7 @@ def make_options(thread_queue_size: int = 128, candidates: int = 0, cp_hashes: i
     o.cp_rounds = cp_rounds
     o.stream = stream
     o.fp64_recheck = fp64_recheck
+    o.sketch_scan = sketch_scan
     return o
 
 
@@ -386,6 +389,7 @@ __all__ = [
     "random_plus_minus", "random_bools", "Index", "merge_topk", "validate", "parse_file", "write_file", "Server",
     "make_options", "launch_count", "profile_enable", "profile_report", "IMPL_EXACT", "IMPL_SIMHASH", "IMPL_WMH",
     "IMPL_WMH_ONEBIT", "IMPL_JL", "IMPL_TC", "IMPL_TC_FP8", "KEYS_SIMHASH", "KEYS_WMH", "KEYS_WMH_ONEBIT", "KEYS_CROSSPOLY",
+    "SKETCH_SCAN_AUTO", "SKETCH_SCAN_POPCOUNT", "SKETCH_SCAN_TENSOR",
     "ANGULAR", "JACCARD", "EUCLIDEAN", "EXPORT_DATA", "EXPORT_SKETCHES", "EXPORT_KEYS", "EXPORT_OFFSETS",
     "EXPORT_BUCKETS", "POINT_DTYPE", "read_truth", "write_truth",
 ]

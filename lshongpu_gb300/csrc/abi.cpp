@@ -156,6 +156,7 @@ void lshg_options_default(lshg_options* opt) {
   opt->cp_rounds = 3;
   opt->stream = nullptr;
   opt->fp64_recheck = -1;
+  opt->sketch_scan = 0;
 }
 
 int lshg_linear_scans_ex(int implementation, int k, int d, int N_query, int N_data, const float* data,

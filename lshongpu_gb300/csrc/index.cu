@@ -15,8 +15,13 @@
 #include "host_rng.h"
 #include "index.h"
 #include "launch_count.h"
+#include "tc_filter.h"
 
 namespace lshg {
+
+// Batches from this many queries up take the tensor-core sketch scan by default (a
+// 128-query tile is the MMA's M; below this most of it would be padding).
+constexpr int kTcSketchMinQueries = 64;
 
 int next_pow2(int v) {
   int p = 1;
@@ -28,6 +33,11 @@ void tile_sketches(Index& I, cudaStream_t s) {
   const int64_t tiles = (I.n + 127) / 128;
   I.xst.alloc((size_t)tiles * 128 * I.wp, s);
   launch_tile_sketches(I.xs.ptr, I.n, I.wp, I.xst.ptr, s);
+  if ((I.sk_kind == 3 || I.sk_kind == 5) && I.words <= 32 && I.p.opt.sketch_scan != 1) {
+    const int64_t rows = (I.n + 255) / 256 * 256;
+    I.xse.alloc((size_t)rows * 128 * tc::hamming_chunks(I.words), s);
+    tc::launch_expand_bits(I.xs.ptr, I.n, I.wp, I.words, rows, I.xse.ptr, s);
+  }
 }
 
 void launch_pack_bytes(const uint8_t* in, int64_t n, int sbytes, uint32_t* out, int wp, uint8_t pad, cudaStream_t s);
@@ -266,7 +276,8 @@ int* Index::error_word(cudaStream_t s) {
 Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
   for (auto& kv : err_words) cudaFree(kv.second);  // cudaFree waits for work that may still write it
-  x.release(); xnorm.release(); xt.release(); xs.release(); xsf.release(); xsft.release(); sk_planes.release();
+  x.release(); xnorm.release(); xt.release(); xs.release(); xse.release(); xsf.release(); xsft.release();
+  sk_planes.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
   xbf.release(); xbf_scale.release(); xf8.release(); xst.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
@@ -567,9 +578,18 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     part.alloc((size_t)nq * splits * C, s);
     launch_scan_float(I.xsft.ptr, I.n, I.sdim, nullptr, qsf.ptr, nq, nullptr, DIST_SQEUCLID, C, splits, part.ptr, s);
   } else {
+    const int op = impl == 3 ? OP_HAMMING : (impl == 4 ? OP_BYTE_JACCARD : OP_ONEBIT_JACCARD);
+    const int mode = I.p.opt.sketch_scan;
+    if (I.xse.ptr && (mode == 2 || (mode == 0 && nq >= kTcSketchMinQueries)) && tc::plan_hamming(I.n, C).ok) {
+      // tensor cores: the exact top-C by (sketch distance, id), then the same re-rank
+      part.alloc((size_t)nq * C, s);
+      tc::launch_tc_hamming(I.xse.ptr, I.n, I.xst.ptr, I.wp, I.words, qs.ptr, nq, op, C, part.ptr, I.error_word(s), s);
+      launch_rerank(part.ptr, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
+                    I.p.opt.fp64_recheck > 0);
+      return;
+    }
     splits = scan_bits_splits(I.n, nq, C);
     part.alloc((size_t)nq * splits * C, s);
-    int op = impl == 3 ? OP_HAMMING : (impl == 4 ? OP_BYTE_JACCARD : OP_ONEBIT_JACCARD);
     launch_scan_bits(I.xst.ptr, I.n, I.wp, I.words, I.sbytes, qs.ptr, nq, op, C, splits, part.ptr, s);
   }
   const uint64_t* cand = part.ptr;

@@ -56,6 +56,8 @@ struct Index {
   int words = 0, wp = 0, sbytes = 0, sdim = 0;
   DevBuf<uint32_t> xs;       // packed sketches, rows of wp words
   DevBuf<uint32_t> xst;      // linear scans: the same, tiled [ceil(N/128)][wp/4][128] x 16 B
+  DevBuf<uint8_t> xse;       // tensor-core sketch scans: sketch bits as E4M3 +-1 rows,
+                             // [ceil(n/256)*256][128 * ceil(words/4)] (derived, not stored)
   DevBuf<float> xsf, xsft;   // JL sketches [n][sdim] and their tile layout
   DevBuf<float> sk_planes;   // SimHash planes [32*sketchDim][d] or JL rows [sdim][d]
   WmhState wmh_sk;
@@ -118,7 +120,8 @@ void sketch_queries(Index& idx, float* q, int nq, DevBuf<uint32_t>* qs, DevBuf<f
 
 int next_pow2(int v);
 
-// Build idx.xst (the linear scans' tiled sketches) from idx.xs.
+// Build idx.xst (the linear scans' tiled sketches) from idx.xs, and for Hamming / one-bit
+// Jaccard sketches of at most 1024 bits idx.xse (their E4M3 rows for the tensor cores).
 void tile_sketches(Index& idx, cudaStream_t stream);
 
 // Persistence (persist.cpp): checksummed binary image of a built index.

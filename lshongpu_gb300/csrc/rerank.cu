@@ -7,11 +7,12 @@
 // produces by writing its sorted warp queue back to front (sketchedDistanceScanners.cuh:
 // 84-99).  Empty candidates (no point) become (-1, INT_MAX) as in the reference.
 //
-// FP64 boundary re-check (optional, on by default for the tensor-core scans): after the
-// FP32 sort, the candidates whose FP32 distance lies within the FP32 error bound of the
-// k-th one are re-scored in double precision and reordered by (FP64 distance, id), so the
-// top-k set and its order at the boundary are those of the exact distances.  Returned
-// distances stay the FP32 values of the reference's formula.
+// FP64 re-check (optional, on by default for the tensor-core scans): after the FP32 sort,
+// the candidates whose FP32 distances lie within the FP32 error bound of a neighbour's --
+// the only ones whose order FP32 may get wrong, at the k-th place or anywhere else -- are
+// re-scored in double precision and reordered by (FP64 distance, id), so the top-k set and
+// its order are those of the exact distances for every k.  Returned distances stay the
+// FP32 values of the reference's formula.
 #include "common.cuh"
 #include "kernels.h"
 #include "launch_count.h"
@@ -62,57 +63,58 @@ __device__ __forceinline__ uint64_t double_to_ordered(double v) {
   return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
-// Reorders keys[lo..hi] (sorted by FP32 key) by FP64 distance, where [lo, hi] holds every
-// candidate whose FP32 distance is within band_abs + band_rel * |kth| of the k-th one.
-// Called by every thread of the block after the sort; qr is the query row.
+// Orders every run of near-tied candidates by FP64 distance.  After the FP32 sort, entry i
+// joins the run of entry i - 1 when their FP32 distances differ by at most the band (twice
+// the FP32 error bound, band_abs + band_rel * |distance|); two entries of different runs
+// are then in exact order, and each run of two or more entries is re-scored in double
+// precision and sorted by (FP64 distance, id).  The list is thus in FP64 order throughout,
+// so every prefix -- the top-k for any k -- is the FP64 top-k of the candidates.  Runs are
+// searched among the first kBandMax entries.  Called by every thread of the block after
+// the sort; qr is the query row.
 template <int DIST>
-__device__ void fp64_boundary(uint64_t* keys, int C, int k, const float* __restrict__ x, int d, const float* qr,
-                              float band_abs, float band_rel) {
-  __shared__ int s_lo, s_hi;
-  __shared__ uint64_t s_ord[kBandMax];
+__device__ void fp64_runs(uint64_t* keys, int C, const float* __restrict__ x, int d, const float* qr, float band_abs,
+                          float band_rel) {
   __shared__ uint64_t s_key[kBandMax];
-  const int kk = imin(k, C) - 1;
-  const uint64_t kth_key = keys[kk];
-  if (kth_key == kEmptyKey) return;  // fewer than k candidates: no boundary (block-uniform)
-  const float kth = key_dist(kth_key);
-  const float band = band_abs + band_rel * fabsf(kth);
-  if (threadIdx.x == 0) {
-    s_lo = kk;
-    s_hi = kk;
-  }
+  __shared__ uint64_t s_ord[kBandMax];
+  __shared__ short s_run[kBandMax];  // first entry of the entry's run
+  __shared__ short s_len[kBandMax];  // length of the entry's run
+  const int L = imin(C, kBandMax);
+  for (int i = threadIdx.x; i < L; i += blockDim.x) s_key[i] = keys[i];
   __syncthreads();
-  for (int i = threadIdx.x; i < C; i += blockDim.x) {
-    const uint64_t key = keys[i];
-    if (key != kEmptyKey && fabsf(key_dist(key) - kth) <= band) {
-      atomicMin(&s_lo, i);
-      atomicMax(&s_hi, i);
+  if (threadIdx.x == 0) {
+    int start = 0;
+    for (int i = 1; i <= L; ++i) {
+      bool join = false;
+      if (i < L && s_key[i] != kEmptyKey && s_key[i - 1] != kEmptyKey) {
+        const float a = key_dist(s_key[i - 1]), b = key_dist(s_key[i]);
+        join = fabsf(b - a) <= band_abs + band_rel * fmaxf(fabsf(a), fabsf(b));
+      }
+      if (!join) {
+        for (int j = start; j < i; ++j) {
+          s_run[j] = (short)start;
+          s_len[j] = (short)(i - start);
+        }
+        start = i;
+      }
     }
   }
   __syncthreads();
-  int lo = s_lo, hi = s_hi;
-  if (hi - lo + 1 > kBandMax) {  // massive near-ties: the kBandMax entries around the k-th
-    lo = imax(lo, kk - (kBandMax / 2 - 1));
-    hi = imin(hi, lo + kBandMax - 1);
-    lo = imax(s_lo, hi - kBandMax + 1);
-  }
-  const int m = hi - lo + 1;
-  if (m < 2) return;  // block-uniform
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    const uint64_t key = keys[lo + t];
-    s_key[t] = key;
-    s_ord[t] = double_to_ordered(fp64_distance<DIST>(x + (int64_t)key_id(key) * d, qr, d));
-  }
+  for (int i = threadIdx.x; i < L; i += blockDim.x)
+    if (s_len[i] > 1) s_ord[i] = double_to_ordered(fp64_distance<DIST>(x + (int64_t)key_id(s_key[i]) * d, qr, d));
   __syncthreads();
-  for (int t = threadIdx.x; t < m; t += blockDim.x) {
-    const uint64_t ot = s_ord[t];
-    const uint32_t it = (uint32_t)key_id(s_key[t]);
+  for (int i = threadIdx.x; i < L; i += blockDim.x) {
+    const int len = s_len[i];
+    if (len < 2) continue;
+    const int r0 = s_run[i];
+    const uint64_t oi = s_ord[i];
+    const uint32_t ii = (uint32_t)key_id(s_key[i]);
     int r = 0;
-    for (int j = 0; j < m; ++j) {
+    for (int j = r0; j < r0 + len; ++j) {
       const uint64_t oj = s_ord[j];
       const uint32_t ij = (uint32_t)key_id(s_key[j]);
-      r += (oj < ot) || (oj == ot && (ij < it || (ij == it && j < t)));
+      r += (oj < oi) || (oj == oi && (ij < ii || (ij == ii && j < i)));
     }
-    keys[lo + r] = s_key[t];
+    keys[r0 + r] = s_key[i];
   }
   __syncthreads();
 }
@@ -163,7 +165,7 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, x, d, qr, band_abs, band_rel);
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -244,7 +246,7 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, x, d, qr, band_abs, band_rel);
   for (int i = tid; i < k; i += CH) {
     const uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;

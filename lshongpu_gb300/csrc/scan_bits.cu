@@ -71,7 +71,8 @@ __device__ __forceinline__ int word_score(uint32_t a, uint32_t b) {
 template <int OP, int QB, int KBUF, int T, int NC, int MINB = 2>
 __global__ void __launch_bounds__(256, MINB) scan_bits_kernel(const uint32_t* __restrict__ xst, int64_t n, int wp, int words,
                                                         int sbytes, const uint32_t* __restrict__ qs, int nq, int C,
-                                                        int tiles_per_split, int splits, uint64_t* __restrict__ out) {
+                                                        int tiles_per_split, int splits, uint64_t* __restrict__ out,
+                                                        const int* __restrict__ list) {
   static_assert(KBUF >= T * kTile, "append buffer must absorb T tiles");
   constexpr int kLimit = KBUF - T * kTile;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -80,7 +81,11 @@ __global__ void __launch_bounds__(256, MINB) scan_bits_kernel(const uint32_t* __
   TopCShared S{reinterpret_cast<uint64_t*>(smem + L.kept), reinterpret_cast<uint64_t*>(smem + L.buf),
                reinterpret_cast<int*>(smem + L.cnt), reinterpret_cast<uint64_t*>(smem + L.thr), C, KBUF};
 
+  // list (optional): scan only the queries list[1 .. list[0]]; slot i of the list is query
+  // list[1 + i], and its result goes to that query's row
+  const int nqe = list ? list[0] : nq;
   const int q0 = blockIdx.x * QB;
+  if (q0 >= nqe) return;  // block-uniform, before any barrier
   const int split = blockIdx.y;
   const int ntiles = (int)((n + kTile - 1) / kTile);
   const int t_begin = split * tiles_per_split;
@@ -90,7 +95,8 @@ __global__ void __launch_bounds__(256, MINB) scan_bits_kernel(const uint32_t* __
 
   for (int i = threadIdx.x; i < QB * wp; i += blockDim.x) {
     int qi = i / wp;
-    qsm[i] = (q0 + qi < nq) ? qs[(int64_t)(q0 + qi) * wp + (i - qi * wp)] : 0u;
+    const int64_t qrow = q0 + qi < nqe ? (list ? list[1 + q0 + qi] : q0 + qi) : 0;
+    qsm[i] = (q0 + qi < nqe) ? qs[qrow * wp + (i - qi * wp)] : 0u;
   }
   topc_init(S, QB);
   __syncthreads();
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(256, MINB) scan_bits_kernel(const uint32_t* __
 #pragma unroll
       for (int a = 0; a < QPT; ++a) {
         const int qi = half + 2 * a;
-        if (qi >= QB || q0 + qi >= nq) continue;
+        if (qi >= QB || q0 + qi >= nqe) continue;
         const uint4* qv = reinterpret_cast<const uint4*>(qsm + qi * wp);
         int acc = 0;
 #pragma unroll
@@ -160,33 +166,36 @@ __global__ void __launch_bounds__(256, MINB) scan_bits_kernel(const uint32_t* __
 
   for (int i = threadIdx.x; i < QB * C; i += blockDim.x) {
     int qi = i / C, c = i - qi * C;
-    if (q0 + qi < nq) out[((int64_t)(q0 + qi) * splits + split) * C + c] = S.kept[(size_t)qi * C + c];
+    if (q0 + qi < nqe) {
+      const int64_t qrow = list ? list[1 + q0 + qi] : q0 + qi;
+      out[(qrow * splits + split) * C + c] = S.kept[(size_t)qi * C + c];
+    }
   }
 }
 
 template <int OP, int QB, int KBUF, int T, int NC, int MINB = 2>
 void launch_cfg(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
-                int splits, uint64_t* out, cudaStream_t s) {
-  ProfScope _ps("scan_bits", s);
+                int splits, uint64_t* out, const int* list, cudaStream_t s) {
+  ProfScope _ps(list ? "scan_bits_listed" : "scan_bits", s);
   size_t smem = bits_layout(wp, QB, C, KBUF).total;
   auto kern = scan_bits_kernel<OP, QB, KBUF, T, NC, MINB>;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int ntiles = ceil_div(n, kTile);
   int tps = ceil_div(ntiles, splits);
   dim3 grid(ceil_div(nq, QB), splits);
-  kern<<<grid, 256, smem, s>>>(xs, n, wp, words, sbytes, qs, nq, C, tps, splits, out);
+  kern<<<grid, 256, smem, s>>>(xs, n, wp, words, sbytes, qs, nq, C, tps, splits, out, list);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
 
 template <int OP, int NC>
 void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
-               int splits, uint64_t* out, cudaStream_t s) {
-  if (C <= 128) launch_cfg<OP, 16, 256, 1, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+               int splits, uint64_t* out, const int* list, cudaStream_t s) {
+  if (C <= 128) launch_cfg<OP, 16, 256, 1, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);
   // up to 1024: 4 queries a block (49 KB at C = 1024) so that three CTAs share an SM and hide
   // one another's fold barriers; the base is streamed twice as often, which L2 absorbs
-  else if (C <= 1024) launch_cfg<OP, 4, 512, 2, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else launch_cfg<OP, 2, 2048, 4, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);  // long folds: fewer
+  else if (C <= 1024) launch_cfg<OP, 4, 512, 2, NC, 3>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);
+  else launch_cfg<OP, 2, 2048, 4, NC>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);  // long folds: fewer
 }
 
 // Row width specialised for each sketch type's usual size (1024-bit SimHash = 8 chunks,
@@ -194,9 +203,9 @@ void launch_op(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, con
 // generic kernel.
 template <int OP, int NC_FAST>
 void launch_width(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int C,
-                  int splits, uint64_t* out, cudaStream_t s) {
-  if (wp / 4 == NC_FAST) launch_op<OP, NC_FAST>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
-  else launch_op<OP, 0>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+                  int splits, uint64_t* out, const int* list, cudaStream_t s) {
+  if (wp / 4 == NC_FAST) launch_op<OP, NC_FAST>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);
+  else launch_op<OP, 0>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);
 }
 
 }  // namespace
@@ -247,21 +256,37 @@ void launch_tile_sketches(const uint32_t* xs, int64_t n, int wp, uint32_t* xst, 
   LSHG_CHECK_LAUNCH();
 }
 
-int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int op,
-                     int C, int splits, uint64_t* out, cudaStream_t s) {
+namespace {
+int scan_bits_dispatch(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq,
+                       int op, int C, int splits, uint64_t* out, const int* list, cudaStream_t s) {
   if (nq <= 0) return splits;
   LSHG_REQUIRE(n > 0, "sketch scan: empty base");
   LSHG_REQUIRE(wp % 4 == 0 && wp / 4 <= kMaxChunks, "sketch scan: rows must be 4..64 words, multiple of 4");
   LSHG_REQUIRE(C >= 32 && C <= 4096 && (C & (C - 1)) == 0, "sketch scan: C must be a power of two in [32, 4096]");
   switch (op) {
-    case OP_HAMMING: launch_width<OP_HAMMING, 8>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
-    case OP_BYTE_JACCARD: launch_width<OP_BYTE_JACCARD, 16>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s); break;
+    case OP_HAMMING: launch_width<OP_HAMMING, 8>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s); break;
+    case OP_BYTE_JACCARD:
+      launch_width<OP_BYTE_JACCARD, 16>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);
+      break;
     case OP_ONEBIT_JACCARD:
-      launch_width<OP_ONEBIT_JACCARD, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, s);
+      launch_width<OP_ONEBIT_JACCARD, 2>(xs, n, wp, words, sbytes, qs, nq, C, splits, out, list, s);
       break;
     default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "sketch scan: invalid sketch type");
   }
   return splits;
+}
+}  // namespace
+
+int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq, int op,
+                     int C, int splits, uint64_t* out, cudaStream_t s) {
+  return scan_bits_dispatch(xs, n, wp, words, sbytes, qs, nq, op, C, splits, out, nullptr, s);
+}
+
+// The queries list[1 .. list[0]] (a device-side list, at most nq of them) scanned over
+// the whole base, each result written to out[query][C]; blocks past the list's end exit.
+int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, const uint32_t* qs, int nq, int op,
+                            int C, const int* list, uint64_t* out, cudaStream_t s) {
+  return scan_bits_dispatch(xst, n, wp, words, 0, qs, nq, op, C, 1, out, list, s);
 }
 
 }  // namespace lshg

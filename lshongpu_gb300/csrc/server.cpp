@@ -4,11 +4,19 @@
 //  * submit() copies the request, checks admission (queue capacity, and enough free HBM
 //    above a reserve for the request's buffers) and enqueues it;
 //  * one scheduler thread owns `streams` launch slots.  Whenever a slot is free it takes
-//    the oldest pending request and coalesces the following requests for the same
-//    (index, k) up to max_batch queries, pads the batch to a power-of-two class by
-//    repeating its last query, copies it into the slot's pinned buffer and launches it;
-//    requests that arrive while other batches are on the GPU go to the next free slot,
-//    so their work overlaps on the device;
+//    the oldest pending request whose index holds fewer than streams - 1 busy slots while
+//    requests for other indexes wait (so long requests on one index cannot occupy every
+//    slot) and coalesces the following
+//    requests for the same index and candidate class up to max_batch queries; a batch of
+//    fewer than max_batch queries waits until its oldest request is batch_window_us old,
+//    so that requests arriving meanwhile join it.  Requests with different k share a
+//    launch when the index computes the same candidates for them (batch_class): the
+//    launch runs at the largest k and each request receives the first k of its rows,
+//    which is its own top-k (the lists are sorted, ties by lower index, and with the FP64
+//    re-check every near-tie run is in FP64 order).  The batch is padded to a power-of-two
+//    class by repeating its last query, copied into the slot's pinned buffer and launched;
+//    requests that arrive while other batches are on the GPU go to the next free slot, so
+//    their work overlaps on the device;
 //  * each (slot, index, k, class) launch is recorded once into a CUDA graph and replayed
 //    afterwards (falling back to direct launches if recording fails);
 //  * a host callback at the end of each slot's stream wakes the scheduler, which splits
@@ -50,6 +58,20 @@ struct Request {
   std::string err;
 };
 
+// Requests whose (index, class) match get the same candidates whatever their k, so they
+// can share a launch run at the largest k.  Tensor-core scans re-rank 64 candidates for
+// k <= 32 and 128 beyond; sketched scans max(C, k rounded up); exact scans and LSH
+// buckets do not depend on k.
+int batch_class(const Index& I, int k) {
+  const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
+  if (I.p.framework == 0 && (impl == 8 || impl == 9)) return k <= 32 ? 0 : 1;
+  int kp = 32;
+  while (kp < k) kp <<= 1;
+  const bool sketched = I.p.framework == 0 ? (impl >= 3 && impl <= 6) : (I.p.runWithSketchedData && I.sk_kind);
+  if (sketched) return std::max(I.C, kp);
+  return 0;
+}
+
 struct Slot {
   cudaStream_t stream = nullptr;
   float* h_in = nullptr;
@@ -60,7 +82,7 @@ struct Slot {
   bool busy = false;
   std::atomic<bool> finished{false};
   std::vector<std::shared_ptr<Request>> batch;
-  int index_id = 0, k = 0, rows = 0;
+  int index_id = 0, k = 0, rows = 0;  // k: the launch's (largest) k
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;  // (index, k, class)
   std::map<std::tuple<int, int, int>, bool> no_graph;
 };
@@ -77,6 +99,7 @@ struct lshg_server {
   std::unordered_map<int64_t, std::shared_ptr<Request>> tickets;
   int64_t next_ticket = 1;
   std::vector<std::unique_ptr<Slot>> slots;
+  std::map<int, int> busy_slots;  // index id -> slots running it
   std::thread worker;
   bool stop = false;
   int64_t completed = 0, launches = 0, replays = 0, rejected = 0;
@@ -157,10 +180,13 @@ struct lshg_server {
   void launch(Slot& s, std::vector<std::shared_ptr<Request>>&& batch) {
     Index& idx = *indexes.at(batch[0]->index_id);
     const int d = idx.d;
-    int rows = 0;
-    for (auto& r : batch) rows += r->nq;
+    int rows = 0, kmax = 0;
+    for (auto& r : batch) {
+      rows += r->nq;
+      kmax = std::max(kmax, r->k);
+    }
     int cls = next_pow2(std::max(1, rows));
-    ensure_buffers(s, (size_t)cls * d, (size_t)cls * batch[0]->k);
+    ensure_buffers(s, (size_t)cls * d, (size_t)cls * kmax);
     float* dst = s.h_in;
     for (auto& r : batch) {
       memcpy(dst, r->q.data(), r->q.size() * sizeof(float));
@@ -170,7 +196,7 @@ struct lshg_server {
     for (int i = rows; i < cls; ++i) memcpy(s.h_in + (size_t)i * d, last, (size_t)d * sizeof(float));
     s.batch = std::move(batch);
     s.index_id = s.batch[0]->index_id;
-    s.k = s.batch[0]->k;
+    s.k = kmax;
     s.rows = rows;
     s.busy = true;
     s.finished.store(false);
@@ -197,11 +223,11 @@ struct lshg_server {
       err = cudaGetErrorString(ce);
     }
     auto now = Clock::now();
-    size_t off = 0;
-    for (auto& r : s.batch) {
-      size_t cnt = (size_t)r->nq * r->k;
-      r->out.assign(s.h_out + off, s.h_out + off + cnt);
-      off += cnt;
+    size_t row = 0;
+    for (auto& r : s.batch) {  // the first r->k of each of the request's rows
+      r->out.resize((size_t)r->nq * r->k);
+      for (int i = 0; i < r->nq; ++i, ++row)
+        memcpy(r->out.data() + (size_t)i * r->k, s.h_out + row * s.k, (size_t)r->k * sizeof(lshg_point));
       r->t_done = now;
       r->status = status;
       r->err = err;
@@ -212,6 +238,54 @@ struct lshg_server {
     s.busy = false;
   }
 
+  // Next batch for a free slot, or empty (then *wait_us is how long until the oldest
+  // eligible request's batching window closes, or -1).  Called with mu held.
+  std::vector<std::shared_ptr<Request>> take_batch(Clock::time_point now, int64_t* wait_us) {
+    *wait_us = -1;
+    // an index keeps one slot free for the others while requests for another index wait
+    bool mixed = false;
+    for (auto& r : queue)
+      if (r->index_id != queue.front()->index_id) {
+        mixed = true;
+        break;
+      }
+    const int cap = (mixed && slots.size() > 1) ? (int)slots.size() - 1 : (int)slots.size();
+    std::shared_ptr<Request> first;
+    for (auto& r : queue)
+      if (busy_slots[r->index_id] < cap) {
+        first = r;
+        break;
+      }
+    if (!first) return {};
+    const Index& I = *indexes.at(first->index_id);
+    const int cls = batch_class(I, first->k);
+    auto same = [&](const Request& r) {
+      return r.index_id == first->index_id && batch_class(*indexes.at(r.index_id), r.k) == cls;
+    };
+    int avail = 0;
+    for (auto& r : queue)
+      if (same(*r)) avail += r->nq;
+    const int64_t age = std::chrono::duration_cast<std::chrono::microseconds>(now - first->t_submit).count();
+    if (p.batch_window_us > 0 && avail < p.max_batch && age < p.batch_window_us) {
+      *wait_us = p.batch_window_us - age;
+      return {};
+    }
+    std::vector<std::shared_ptr<Request>> batch;
+    int rows = 0;
+    for (auto it = queue.begin(); it != queue.end();) {
+      auto& r = *it;
+      if (same(*r) && rows + r->nq <= p.max_batch) {
+        rows += r->nq;
+        r->state = 1;
+        batch.push_back(r);
+        it = queue.erase(it);
+      } else {
+        ++it;
+      }
+    }
+    return batch;
+  }
+
   void loop() {
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lk(mu);
@@ -220,30 +294,27 @@ struct lshg_server {
       for (auto& sp : slots) {
         Slot& s = *sp;
         if (s.busy && s.finished.load()) {
+          const int iid = s.index_id;
           lk.unlock();
           finish(s);
           lk.lock();
+          --busy_slots[iid];
           progressed = true;
           cv_done.notify_all();
         }
       }
+      int64_t wait_us = -1;
       for (auto& sp : slots) {
         Slot& s = *sp;
         if (s.busy || queue.empty()) continue;
-        std::vector<std::shared_ptr<Request>> batch;
-        auto first = queue.front();
-        int rows = 0;
-        for (auto it = queue.begin(); it != queue.end();) {
-          auto& r = *it;
-          if (r->index_id == first->index_id && r->k == first->k && rows + r->nq <= p.max_batch) {
-            rows += r->nq;
-            r->state = 1;
-            batch.push_back(r);
-            it = queue.erase(it);
-          } else {
-            ++it;
-          }
+        int64_t w = -1;
+        auto batch = take_batch(Clock::now(), &w);
+        if (batch.empty()) {
+          if (w >= 0 && (wait_us < 0 || w < wait_us)) wait_us = w;
+          continue;
         }
+        const int iid = batch[0]->index_id;
+        ++busy_slots[iid];
         lk.unlock();
         try {
           launch(s, std::move(batch));
@@ -258,6 +329,7 @@ struct lshg_server {
           cudaGetLastError();
         }
         lk.lock();
+        if (!s.busy) --busy_slots[iid];
         progressed = true;
         cv_done.notify_all();
       }
@@ -266,7 +338,9 @@ struct lshg_server {
         for (auto& sp : slots) any = any || sp->busy;
         if (!any) break;
       }
-      if (!progressed) cv_work.wait_for(lk, std::chrono::microseconds(200));
+      if (!progressed)
+        cv_work.wait_for(lk, std::chrono::microseconds(wait_us >= 0 ? std::max<int64_t>(1, std::min<int64_t>(wait_us, 200))
+                                                                    : 200));
     }
   }
 };

@@ -624,15 +624,7 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
       if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64, false>(ma, mb, mbhi, a, "tc_prepass", s);
       else run_filter<MODE_GROUPMAX, 8, false>(ma, mb, mbhi, a, "tc_prepass", s);
     }
-    {
-      ProfScope _ps("tc_tau_select", s);
-      if (plan.M <= 32 * kTauRegs && plan.M % 4 == 0)
-        tau_select_reg_kernel<kTauRegs><<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, margin, tau);
-      else
-        tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax.ptr, nq, plan.M, CT, margin, tau);
-      count_launch();
-      LSHG_CHECK_LAUNCH();
-    }
+    launch_tau_select(gmax.ptr, nq, plan.M, CT, margin, tau, s);
   }
   a.gmax = nullptr;
   a.M = 0;
@@ -646,12 +638,23 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
   else run_filter<MODE_FILTER, 64, false>(ma, mb, mbhi, a, "tc_filter", s);
 }
 
+void launch_tau_select(const float* gmax, int nq, int M, int rank, float margin, float* tau, cudaStream_t s) {
+  ProfScope _ps("tc_tau_select", s);
+  if (M <= 32 * kTauRegs && M % 4 == 0)
+    tau_select_reg_kernel<kTauRegs><<<ceil_div(nq, 8), 256, 0, s>>>(gmax, nq, M, rank, margin, tau);
+  else
+    tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax, nq, M, rank, margin, tau);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
                         cudaStream_t s) {
   ProfScope _ps("tc_cand_select", s);
-  if (CT == 64) cand_select_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
+  if (CT == 32) cand_select_kernel<1><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
+  else if (CT == 64) cand_select_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
   else if (CT == 128) cand_select_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
-  else throw Error(LSHG_ERR_INVALID_ARGUMENT, "tensor-core scan: candidate count must be 64 or 128");
+  else throw Error(LSHG_ERR_INVALID_ARGUMENT, "tensor-core scan: candidate count must be 32, 64 or 128");
   count_launch();
   LSHG_CHECK_LAUNCH();
 }

@@ -38,9 +38,40 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
                         const FilterPlan& plan, int nq, int64_t n, int d, int QT, int CT, float* tau, int* cnt,
                         uint64_t* cand, int* err, bool e4m3, cudaStream_t s);
 
-// Top-CT keys a query from its survivors; overflowed queries are listed in ovf.
+// tau[q] = a lower bound (within 1/65536 of the row's range) of the rank-th largest of the
+// row's M group maxima, minus margin; -inf when the row holds fewer than rank maxima.
+void launch_tau_select(const float* gmax, int nq, int M, int rank, float margin, float* tau, cudaStream_t s);
+
+// Top-CT keys a query from its survivors (CT = 32, 64 or 128); overflowed queries are
+// listed in ovf.
 void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
                         cudaStream_t s);
+
+// Tensor-core sketch scan (tc_hamming.cu): threshold plan for a base of n points and the
+// top-C of each query.  ok = false: no prepass shape bounds C well (use the popcount scan).
+struct HammingPlan {
+  bool ok;
+  int NT;    // 256-point base tiles
+  int GW;    // prepass group width (64 or 8; 0 = no prepass, every point survives)
+  int S;     // prepass samples every S-th tile
+  int NS;    // sampled tiles
+  int M;     // group maxima a query
+  int rank;  // tau = the rank-th largest maximum
+  int cap;   // survivor slots a query
+};
+HammingPlan plan_hamming(int64_t n, int C);
+// 128-bit chunks of a sketch row of `words` words (rows of 128 * chunks E4M3 bytes).
+int hamming_chunks(int words);
+// Sketch rows [n][wp] (first `words` real) -> E4M3 +-1 rows [rows_pad][128 * chunks].
+void launch_expand_bits(const uint32_t* xs, int64_t n, int wp, int words, int64_t rows_pad, uint8_t* out,
+                        cudaStream_t s);
+// Top-C keys [nq][C] of each query by (hamming asc, id asc); xse: the base's E4M3 rows
+// (launch_expand_bits, rows padded to 256), xst: the tiled sketches (listed rescans), qs:
+// query sketches [nq][wp].  op: OP_HAMMING or OP_ONEBIT_JACCARD.
+void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int wp, int words, const uint32_t* qs,
+                       int nq, int op, int C, uint64_t* out, int* err, cudaStream_t s);
+// Rows of kp bytes (a multiple of 16); boxes of 128 bytes x box_rows rows, 128-byte swizzle.
+CUtensorMap make_map_bytes(const void* base, int64_t rows, int kp, int box_rows);
 
 void launch_gather_rows(const uint16_t* src, const int* ovf, int nq, uint16_t* dst, cudaStream_t s);
 

@@ -1,0 +1,595 @@
+// Tensor-core sketch scan: the Hamming distance of bit sketches as a +-1 E4M3 GEMM
+// (implementations 3 and 5 -- SimHash and one-bit weighted MinHash -- in place of the
+// XOR/popcount scan of scan_bits.cu for batches that fill the tensor cores; the
+// reference's scanHammingDistance, sketchedDistanceScanners.cuh:14-100, and its one-bit
+// scanJaccardDistance, :194-274).
+//
+// Bit b of a sketch becomes the E4M3 value 1 - 2b: +1.0 (0x38) or -1.0 (0xB8).  For two
+// sketches of B = 32 * words bits the dot product of those rows is (#equal bits) -
+// (#different bits) = B - 2 * hamming.  Every product is +-1 and every partial sum an
+// integer of magnitude <= B <= 1024, which FP32 holds exactly, so the accumulator gives
+// hamming = (B - dot) / 2 exactly, and the top-C by (hamming, id) equals the popcount
+// scan's.  The one-bit Jaccard distance 1 - (B - hamming) / B orders points the same way.
+// Rows are padded to whole 128-byte chunks with 0x00 (+0.0), which adds nothing.
+//
+// Selection, as in the threshold-filter scan of tc_filter.cu, in two GEMM passes:
+//   prepass  on every S-th base tile writes each query's group maxima of the score (the
+//            best score of each 64- or 8-point group of a sampled tile); tau[q] = the
+//            r-th largest of them (launch_tau_select).  With S = 1, r = C and every point
+//            of the exact top-C scores >= tau.  With S > 1, r = C/S + 4 sqrt(C/S) + 8 -- the
+//            C-th best point of the base would put about C/S points of the sample above
+//            it, so tau stays at or below it unless that count exceeds its mean by four
+//            standard deviations -- and about r * S ~ 1.5 C points survive instead of C * S;
+//   filter   on the whole base keeps the points whose score reaches tau[q], staged per row
+//            in shared memory and moved to the query's candidate array with one atomicAdd
+//            a batch;
+//   select   sorts each query's survivors by (score desc, id asc) and keeps the first C.
+//            A query with fewer than C survivors (tau above its C-th best score: the
+//            sample was unrepresentative) or more than its array holds (massive ties) is
+//            listed and rescanned exactly by the popcount scan on the device, so the result
+//            is always the exact top-C.
+//
+// tc_hamming_kernel: persistent, one CTA per SM, 640 threads.  A unit is (query tile of 128
+// rows, chunk of up to 32 consecutive base tiles of 256 points), numbered chunk-major so
+// that all SMs stream the same base tiles at a time (each read from HBM about once a batch,
+// then from L2).  The query tile stays in shared memory for the unit (KC chunks of 128 rows
+// x 128 bytes); the base tile streams through a ring of one-chunk stages (256 rows x 128
+// bytes).  Warp 0 issues the TMA copies, warp 1 the MMAs (tcgen05.mma kind::f8f6f4, A and
+// B both E4M3, M = 128, N = 256, K = 32 each; 4 a chunk, 4 * KC a tile), warp 2 owns the
+// 512 TMEM columns (two 256-column FP32 accumulators), warps 4-19 are the epilogue
+// (warpgroup g reads columns [64g, 64g + 64), one query row a thread).  Every mbarrier
+// wait is bounded (2 s); a CTA that times out raises error 2, drains its copies and MMAs,
+// frees TMEM and returns.
+#include "index.h"
+#include "launch_count.h"
+#include "profile.h"
+#include "select.cuh"
+#include "tc_filter.h"
+#include "tc_ptx.cuh"
+
+namespace lshg {
+
+int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, const uint32_t* qs, int nq, int op,
+                            int C, const int* list, uint64_t* out, cudaStream_t s);
+
+namespace tc {
+
+namespace {
+
+constexpr int H_THREADS = 640;
+constexpr int HN = 256;           // base points a tile (UMMA N)
+constexpr int H_CHUNK = 128;      // bytes of a row in one K chunk (one 128-byte swizzle row)
+constexpr int H_NACC = 2;         // TMEM accumulators of HN columns
+constexpr int H_TMEM_COLS = H_NACC * HN;
+constexpr int H_EPI_WARPS = 16;
+constexpr int H_SEL_MAX = 16384;  // survivors a query the block select sorts at most
+constexpr int kHTauRegs = 80;
+
+constexpr int kSmemLimit = 232448;  // dynamic shared memory a CTA may opt into
+
+// Shared-memory layout for rows of KC chunks.  The survivor staging takes what is left
+// (8, 4, 2 or 1 entries a row and warpgroup; none: each survivor takes its own slot).
+template <int KC>
+struct HLayout {
+  static constexpr int A_BYTES = KC * BM * H_CHUNK;  // resident query tile
+  static constexpr int B_BYTES = HN * H_CHUNK;       // one chunk of a base tile: 32 KB
+  static constexpr int STAGES = KC <= 4 ? 4 : 3;
+  static constexpr int FIXED = A_BYTES + STAGES * B_BYTES + 256 + 1024;  // + barriers + alignment slack
+  static constexpr int ROOM = (kSmemLimit - FIXED) / (4 * BM * 8);
+  static constexpr int SBUF = ROOM >= 8 ? 8 : ROOM >= 4 ? 4 : ROOM >= 2 ? 2 : ROOM >= 1 ? 1 : 0;
+  static constexpr int A_OFF = 0;
+  static constexpr int B_OFF = A_BYTES;
+  static constexpr int S_OFF = B_OFF + STAGES * B_BYTES;  // scores then ids, [4][SBUF][BM] each
+  static constexpr int BAR_OFF = S_OFF + 4 * SBUF * BM * 8;
+  static constexpr int SMEM = BAR_OFF + 256 + 1024;
+  static_assert(SMEM <= kSmemLimit, "shared memory per CTA");
+  static_assert(8 * (2 * STAGES + 2 + 2 * H_NACC + 1) + 8 <= 256, "barrier area");
+};
+
+struct HArgs {
+  int nq;
+  int64_t n;
+  int QT;           // query tiles
+  int NP;           // base positions scanned (base tile = p * dstride)
+  int dstride;
+  int CH;           // positions a unit
+  int NCH;          // chunks of positions
+  float* gmax;      // MODE_GROUPMAX: [nq][M] group maxima
+  int M;
+  const float* tau; // MODE_FILTER: threshold a query (nullptr: keep every point)
+  int* cnt;         // survivors a query
+  uint64_t* cand;   // [nq][cap] survivor keys
+  int cap;
+  int* err;
+};
+
+__device__ __forceinline__ void h_flush(int* cnt, uint64_t* dst, int cap, const float* ssc, const int* sid,
+                                        int& scnt) {
+  if (scnt > 0) {
+    const int base = atomicAdd(cnt, scnt);
+    for (int e = 0; e < scnt; ++e)
+      if (base + e < cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
+    scnt = 0;
+  }
+}
+
+template <int MODE, int GW, int KC>
+__global__ void __launch_bounds__(H_THREADS, 1)
+    tc_hamming_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                      const HArgs a) {
+  using LY = HLayout<KC>;
+  constexpr int STAGES = LY::STAGES, SBUF = LY::SBUF;
+  static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column pieces");
+  static_assert(GW == 64 || GW == 8, "group width");
+  const int U = a.NCH * a.QT;
+  if ((int)blockIdx.x >= U) return;  // no unit for this CTA: leave before any barrier or TMEM use
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t s0 = smem_u32(sm);
+  const uint32_t bar0 = s0 + LY::BAR_OFF;
+  auto FULL = [&](int s) { return bar0 + 8u * s; };
+  auto EMPTY = [&](int s) { return bar0 + 8u * (STAGES + s); };
+  const uint32_t A_FULL = bar0 + 8u * (2 * STAGES);
+  const uint32_t A_EMPTY = bar0 + 8u * (2 * STAGES + 1);
+  auto ACC_FULL = [&](int b) { return bar0 + 8u * (2 * STAGES + 2 + b); };
+  auto ACC_EMPTY = [&](int b) { return bar0 + 8u * (2 * STAGES + 2 + H_NACC + b); };
+  const uint32_t DONE = bar0 + 8u * (2 * STAGES + 2 + 2 * H_NACC);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + LY::BAR_OFF + 8 * (2 * STAGES + 3 + 2 * H_NACC));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(FULL(s), 1);
+      mbar_init(EMPTY(s), 1);
+    }
+    mbar_init(A_FULL, 1);
+    mbar_init(A_EMPTY, 1);
+    for (int b = 0; b < H_NACC; ++b) {
+      mbar_init(ACC_FULL(b), 1);
+      mbar_init(ACC_EMPTY(b), H_EPI_WARPS);
+    }
+    mbar_init(DONE, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), H_TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0, ua = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
+        const int qt = u % a.QT, c = u / a.QT;
+        const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
+        // one query-tile buffer: the previous unit's MMAs must have completed
+        if (!mbar_wait(A_EMPTY, (ua & 1) ^ 1, abort_flag)) break;
+        mbar_expect_tx(A_FULL, LY::A_BYTES);
+#pragma unroll
+        for (int kc = 0; kc < KC; ++kc)
+          tma_load_2d(s0 + LY::A_OFF + kc * BM * H_CHUNK, &mapA, kc * H_CHUNK, qt * BM, A_FULL);
+        for (int p = p0; p < p1 && ok; ++p) {
+          const int row = p * a.dstride * HN;
+          for (int kc = 0; kc < KC; ++kc) {
+            const int st = it % STAGES, rd = it / STAGES;
+            if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
+            mbar_expect_tx(FULL(st), LY::B_BYTES);
+            tma_load_2d(s0 + LY::B_OFF + st * LY::B_BYTES, &mapB, kc * H_CHUNK, row, FULL(st));
+            ++it;
+          }
+        }
+      }
+      // drain: every issued copy has landed before the CTA may exit
+      for (int j = max(0, it - STAGES); j < it; ++j) mbar_wait(FULL(j % STAGES), (j / STAGES) & 1, abort_flag, true);
+      if (ua > 0) mbar_wait(A_FULL, (ua - 1) & 1, abort_flag, true);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_e4m3(BM, HN);
+      int it = 0, ia = 0, ua = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
+        const int c = u / a.QT;
+        const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
+        if (!mbar_wait(A_FULL, ua & 1, abort_flag)) break;
+        tc_fence_after();
+        for (int p = p0; p < p1 && ok; ++p) {
+          const int b = ia % H_NACC, ub = ia / H_NACC;
+          if (!mbar_wait(ACC_EMPTY(b), (ub & 1) ^ 1, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t d_tmem = tmem + (uint32_t)(b * HN);
+          for (int kc = 0; kc < KC; ++kc) {
+            const int st = it % STAGES, rd = it / STAGES;
+            if (!mbar_wait(FULL(st), rd & 1, abort_flag)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t a_base = s0 + LY::A_OFF + kc * BM * H_CHUNK;
+            const uint32_t b_base = s0 + LY::B_OFF + st * LY::B_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < H_CHUNK / 32; ++kk)
+              umma_e4m3(d_tmem, smem_desc(a_base + kk * 32), smem_desc(b_base + kk * 32), idesc,
+                        (kc > 0 || kk > 0) ? 1u : 0u);
+            umma_commit(EMPTY(st));
+            ++it;
+          }
+          if (!ok) break;
+          umma_commit(ACC_FULL(b));
+          ++ia;
+        }
+        umma_commit(A_EMPTY);  // the query tile is free once this unit's MMAs complete
+      }
+      // drain: all issued MMAs complete before TMEM is released
+      umma_commit(DONE);
+      mbar_wait(DONE, 0, abort_flag, true);
+    }
+    __syncwarp();
+  } else if (warp >= 4) {
+    // ---------------- epilogue ----------------
+    const int g = (warp - 4) >> 2;         // warpgroup: columns [64g, 64g+64) of every accumulator
+    const int r = (warp & 3) * 32 + lane;  // query row within the tile = TMEM lane
+    const uint32_t tbase = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(g * 64);
+    float* ssc = reinterpret_cast<float*>(sm + LY::S_OFF) + (size_t)g * SBUF * BM + r;
+    int* sid = reinterpret_cast<int*>(sm + LY::S_OFF + 4 * SBUF * BM * 4) + (size_t)g * SBUF * BM + r;
+    int scnt = 0;
+    int ia = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < U && ok; u += gridDim.x) {
+      const int qt = u % a.QT, c = u / a.QT;
+      const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
+      const int q = qt * BM + r;
+      float tau = INFINITY;
+      if (MODE == MODE_FILTER && q < a.nq) tau = a.tau ? a.tau[q] : -INFINITY;
+      for (int p = p0; p < p1; ++p) {
+        const int b = ia % H_NACC, ub = ia / H_NACC;
+        if (!mbar_wait(ACC_FULL(b), ub & 1, abort_flag)) { ok = false; break; }
+        tc_fence_after();
+        uint32_t v[64];
+        tmem_ld64(tbase + (uint32_t)(b * HN), v);
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(ACC_EMPTY(b));  // scores are in registers: the MMA may reuse the buffer
+        ++ia;
+        const int64_t cbase = (int64_t)p * a.dstride * HN + g * 64;  // base id of v[0]
+        const int piece = 4 * p + g;
+        if (MODE == MODE_GROUPMAX) {
+          if (cbase + 64 > a.n) {  // last base tile: padding rows are not points
+#pragma unroll
+            for (int j = 0; j < 64; ++j)
+              if (cbase + j >= a.n) v[j] = __float_as_uint(-INFINITY);
+          }
+          if (q < a.nq) {
+            if (GW == 64) {
+              float m[8];
+#pragma unroll
+              for (int gg = 0; gg < 8; ++gg) m[gg] = max8(v, gg);
+              a.gmax[(int64_t)q * a.M + piece] =
+                  max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]), fmaxf(m[6], m[7]));
+            } else {
+              float4 lo, hi;
+              lo.x = max8(v, 0); lo.y = max8(v, 1); lo.z = max8(v, 2); lo.w = max8(v, 3);
+              hi.x = max8(v, 4); hi.y = max8(v, 5); hi.z = max8(v, 6); hi.w = max8(v, 7);
+              float4* dst = reinterpret_cast<float4*>(a.gmax + (int64_t)q * a.M + 8 * piece);
+              dst[0] = lo;
+              dst[1] = hi;
+            }
+          }
+        } else {
+          if (cbase + 64 > a.n) {  // padding rows become NaN, which never passes
+#pragma unroll
+            for (int j = 0; j < 64; ++j)
+              if (cbase + j >= a.n) v[j] = 0x7fc00000u;
+          }
+          float m[8];
+#pragma unroll
+          for (int gg = 0; gg < 8; ++gg) m[gg] = max8(v, gg);
+          const float tm = max3f(max3f(m[0], m[1], m[2]), max3f(m[3], m[4], m[5]), fmaxf(m[6], m[7]));
+          if (__any_sync(0xffffffffu, tm >= tau)) {
+            const int ibase = (int)cbase;  // ids fit in 32 bits (n < 2^31)
+            int* qcnt = a.cnt + q;
+            uint64_t* qdst = a.cand + (int64_t)q * a.cap;
+#pragma unroll
+            for (int gg = 0; gg < 8; ++gg) {
+              if (!__any_sync(0xffffffffu, m[gg] >= tau)) continue;
+              if (SBUF > 0) {
+                int ng = 0;
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) ng += __uint_as_float(v[8 * gg + jj]) >= tau ? 1 : 0;
+                if (scnt + ng > SBUF) h_flush(qcnt, qdst, a.cap, ssc, sid, scnt);
+              }
+#pragma unroll
+              for (int jj = 0; jj < 8; ++jj) {
+                const float sc = __uint_as_float(v[8 * gg + jj]);
+                if (sc >= tau) {
+                  if (SBUF > 0 && scnt < SBUF) {
+                    ssc[scnt * BM] = sc;
+                    sid[scnt * BM] = ibase + 8 * gg + jj;
+                    ++scnt;
+                  } else {  // no staging room: a slot of its own
+                    const int pos = atomicAdd(qcnt, 1);
+                    if (pos < a.cap) qdst[pos] = make_key(-sc, ibase + 8 * gg + jj);
+                  }
+                }
+              }
+            }
+          }
+        }
+      }
+      if (MODE == MODE_FILTER && SBUF > 0 && scnt > 0)  // the next unit is another query tile
+        h_flush(a.cnt + q, a.cand + (int64_t)q * a.cap, a.cap, ssc, sid, scnt);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2) {
+    tc_fence_after();
+    tmem_dealloc(tmem, H_TMEM_COLS);
+  }
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(a.err, 2);
+}
+
+// Sketch rows of wp words (the first `words` real) -> E4M3 rows of kp bytes: bit b of word w
+// (LSB first) -> byte 32w + b = 0x38 (+1) for a 0 bit, 0xB8 (-1) for a 1 bit; bytes past
+// 32 * words and rows past n are 0x00.  One thread writes 16 bytes (half a word).
+__global__ void expand_bits_kernel(const uint32_t* __restrict__ xs, int64_t n, int wp, int words, int kp,
+                                   int64_t rows_pad, uint4* __restrict__ out) {
+  const int per_row = kp / 16;
+  const int64_t total = rows_pad * per_row;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / per_row;
+    const int h = (int)(t - i * per_row);  // 16-byte piece of the row: bits 16h .. 16h + 15
+    const int w = h >> 1;
+    uint4 o = make_uint4(0, 0, 0, 0);
+    if (i < n && w < words) {
+      const uint32_t bits = xs[i * wp + w] >> (16 * (h & 1));
+      uint32_t r[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const uint32_t nib = (bits >> (4 * e)) & 0xFu;
+        // bit j of the nibble -> bit 7 of byte j (the sign of +-1.0)
+        const uint32_t spread = (nib & 1u) << 7 | (nib & 2u) << 14 | (nib & 4u) << 21 | (nib & 8u) << 28;
+        r[e] = 0x38383838u | spread;
+      }
+      o = make_uint4(r[0], r[1], r[2], r[3]);
+    }
+    out[t] = o;
+  }
+}
+
+// Top-C (C <= 128) of each query's survivors, one warp a query; a query whose survivor count
+// is below `need` or above `cap` is listed in ovf (ovf[0] = count, ovf[1..] = queries).
+template <int E>
+__global__ void __launch_bounds__(256) hsel_warp_kernel(const int* __restrict__ cnt, const uint64_t* __restrict__ cand,
+                                                        int cap, int need, int nq, uint64_t* __restrict__ out,
+                                                        int* __restrict__ ovf) {
+  constexpr int CT = 32 * E;
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (q >= nq) return;  // warp-uniform
+  const int c = cnt[q];
+  uint64_t* dst = out + (int64_t)q * CT;
+  if (c > cap || c < need) {
+    if (lane == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
+    return;  // the rescan writes this row
+  }
+  const uint64_t* src = cand + (int64_t)q * cap;
+  uint64_t best[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) best[e] = kEmptyKey;
+  for (int base = 0; base < c; base += CT) {
+    uint64_t x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int i = base + e * 32 + lane;
+      x[e] = i < c ? src[i] : kEmptyKey;
+    }
+    warp_bitonic<E>(x, lane, false);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const uint64_t rr = __shfl_sync(0xffffffffu, x[E - 1 - e], 31 - lane);
+      best[e] = best[e] < rr ? best[e] : rr;
+    }
+    warp_bitonic<E>(best, lane, true);
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) dst[e * 32 + lane] = best[e];
+}
+
+// Top-C (C > 128) of each query's survivors, one block a query: the survivors (at most
+// cap <= H_SEL_MAX) sorted in shared memory, the first C written.  Same listing rule.
+__global__ void __launch_bounds__(512) hsel_block_kernel(const int* __restrict__ cnt,
+                                                         const uint64_t* __restrict__ cand, int cap, int need, int C,
+                                                         uint64_t* __restrict__ out, int* __restrict__ ovf) {
+  extern __shared__ uint64_t keys[];
+  const int q = blockIdx.x;
+  const int c = cnt[q];
+  if (c > cap || c < need) {
+    if (threadIdx.x == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
+    return;
+  }
+  int P = 64;
+  while (P < c || P < C) P <<= 1;
+  const uint64_t* src = cand + (int64_t)q * cap;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) keys[i] = i < c ? src[i] : kEmptyKey;
+  __syncthreads();
+  block_bitonic_sort(keys, P);
+  for (int i = threadIdx.x; i < C; i += blockDim.x) out[(int64_t)q * C + i] = keys[i];
+}
+
+// Rows of kp bytes (a multiple of 128); boxes of 128 bytes x box_rows rows, 128-byte swizzle.
+CUtensorMap map_sketch_rows(const void* base, int64_t rows, int kp, int box_rows) {
+  LSHG_REQUIRE(((uintptr_t)base & 15) == 0 && kp % H_CHUNK == 0, "sketch rows: 16-byte base, 128-byte rows");
+  return make_map_bytes(base, rows, kp, box_rows);
+}
+
+template <int MODE, int GW, int KC>
+void run_hamming(const CUtensorMap& ma, const CUtensorMap& mb, HArgs a, const char* name, cudaStream_t s) {
+  const int G = num_sms();
+  const int64_t work = (int64_t)a.NP * a.QT;
+  a.CH = (int)std::max<int64_t>(1, std::min<int64_t>(32, (work + 8 * G - 1) / (8 * G)));
+  a.NCH = ceil_div(a.NP, a.CH);
+  const int U = a.NCH * a.QT;
+  const int grid = std::min(G, U);
+  auto kern = tc_hamming_kernel<MODE, GW, KC>;
+  constexpr int smem = HLayout<KC>::SMEM;
+  LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ProfScope _ps(name, s);
+  kern<<<grid, H_THREADS, smem, s>>>(ma, mb, a);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+template <int MODE, int GW>
+void run_hamming_kc(int kc, const CUtensorMap& ma, const CUtensorMap& mb, const HArgs& a, const char* name,
+                    cudaStream_t s) {
+  switch (kc) {
+    case 1: run_hamming<MODE, GW, 1>(ma, mb, a, name, s); break;
+    case 2: run_hamming<MODE, GW, 2>(ma, mb, a, name, s); break;
+    case 3: run_hamming<MODE, GW, 3>(ma, mb, a, name, s); break;
+    case 4: run_hamming<MODE, GW, 4>(ma, mb, a, name, s); break;
+    case 5: run_hamming<MODE, GW, 5>(ma, mb, a, name, s); break;
+    case 6: run_hamming<MODE, GW, 6>(ma, mb, a, name, s); break;
+    case 7: run_hamming<MODE, GW, 7>(ma, mb, a, name, s); break;
+    case 8: run_hamming<MODE, GW, 8>(ma, mb, a, name, s); break;
+    default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "tensor-core sketch scan: rows of 1..8 chunks of 128 bits");
+  }
+}
+
+}  // namespace
+
+HammingPlan plan_hamming(int64_t n, int C) {
+  HammingPlan p{};
+  p.ok = true;
+  const int NT = ceil_div(n, HN);
+  p.NT = NT;
+  p.GW = 0;
+  p.S = 1;
+  p.NS = 0;
+  p.M = 0;
+  p.rank = C;
+  if ((int64_t)NT * HN <= (C <= 128 ? 8192 : H_SEL_MAX)) {  // small base: every point survives
+    p.cap = NT * HN;
+    return p;
+  }
+  for (int S : {8, 4, 2, 1}) {
+    const int NS = ceil_div(NT, S);
+    const double m = (double)C / S;
+    const int r = S == 1 ? C : std::min(C, (int)std::ceil(m + 4.0 * std::sqrt(m) + 8.0));
+    for (int GW : {64, 8}) {
+      const int64_t M = (int64_t)NS * (HN / GW);
+      if (M >= 4 * (int64_t)r) {
+        p.S = S;
+        p.NS = NS;
+        p.GW = GW;
+        p.M = (int)M;
+        p.rank = r;
+        const int64_t want = 3 * (int64_t)r * S + 2048;
+        int64_t cap = 1024;
+        while (cap < want) cap <<= 1;
+        if (C > 128) cap = std::min<int64_t>(cap, H_SEL_MAX);
+        p.cap = (int)std::min<int64_t>(cap, (int64_t)NT * HN);
+        return p;
+      }
+    }
+  }
+  // fewer than 4 C group maxima even without sampling: the popcount scan serves it
+  p.ok = false;
+  return p;
+}
+
+int hamming_chunks(int words) { return (words + 3) / 4; }
+
+void launch_expand_bits(const uint32_t* xs, int64_t n, int wp, int words, int64_t rows_pad, uint8_t* out,
+                        cudaStream_t s) {
+  const int kp = hamming_chunks(words) * H_CHUNK;
+  const int64_t total = rows_pad * (kp / 16);
+  if (total <= 0) return;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
+  expand_bits_kernel<<<blocks, 256, 0, s>>>(xs, n, wp, words, kp, rows_pad, reinterpret_cast<uint4*>(out));
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int wp, int words, const uint32_t* qs,
+                       int nq, int op, int C, uint64_t* out, int* err, cudaStream_t s) {
+  if (nq <= 0) return;
+  LSHG_REQUIRE(words >= 1 && words <= 32, "tensor-core sketch scan: 1..32 words a sketch");
+  LSHG_REQUIRE(C >= 32 && C <= 4096 && (C & (C - 1)) == 0, "tensor-core sketch scan: C must be a power of two");
+  const int kc = hamming_chunks(words), kp = kc * H_CHUNK;
+  const int64_t qpad = (int64_t)ceil_div(nq, BM) * BM;
+  const int QT = (int)(qpad / BM);
+  const int64_t npad = (int64_t)ceil_div(n, HN) * HN;
+  const HammingPlan plan = plan_hamming(n, C);
+  LSHG_REQUIRE(plan.ok, "tensor-core sketch scan: C too large for this base");
+  LSHG_REQUIRE((int64_t)QT * plan.NT < (int64_t)INT_MAX, "tensor-core sketch scan: problem too large");
+  DevBuf<uint8_t> qe((size_t)qpad * kp, s);
+  {
+    ProfScope _ps("tc_hamming_expand", s);
+    launch_expand_bits(qs, nq, wp, words, qpad, qe.ptr, s);
+  }
+  const CUtensorMap ma = map_sketch_rows(qe.ptr, qpad, kp, BM);
+  const CUtensorMap mb = map_sketch_rows(xse, npad, kp, HN);
+  HArgs a{};
+  a.nq = nq;
+  a.n = n;
+  a.QT = QT;
+  a.err = err;
+  DevBuf<float> tau(nq, s);
+  if (plan.M > 0) {
+    DevBuf<float> gmax((size_t)nq * plan.M, s);
+    a.NP = plan.NS;
+    a.dstride = plan.S;
+    a.gmax = gmax.ptr;
+    a.M = plan.M;
+    if (plan.GW == 64) run_hamming_kc<MODE_GROUPMAX, 64>(kc, ma, mb, a, "tc_hamming_prepass", s);
+    else run_hamming_kc<MODE_GROUPMAX, 8>(kc, ma, mb, a, "tc_hamming_prepass", s);
+    // scores are integers, computed the same way in both passes: no margin
+    launch_tau_select(gmax.ptr, nq, plan.M, plan.rank, 0.0f, tau.ptr, s);
+  }
+  DevBuf<int> cnt(nq, s);
+  LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes(), s));
+  DevBuf<uint64_t> cand((size_t)nq * plan.cap, s);
+  a.gmax = nullptr;
+  a.M = 0;
+  a.NP = plan.NT;
+  a.dstride = 1;
+  a.tau = plan.M > 0 ? tau.ptr : nullptr;
+  a.cnt = cnt.ptr;
+  a.cand = cand.ptr;
+  a.cap = plan.cap;
+  run_hamming_kc<MODE_FILTER, 64>(kc, ma, mb, a, "tc_hamming", s);
+  DevBuf<int> ovf((size_t)nq + 1, s);
+  LSHG_CUDA(cudaMemsetAsync(ovf.ptr, 0, sizeof(int), s));
+  const int need = (int)std::min<int64_t>(C, n);
+  {
+    ProfScope _ps("tc_hamming_select", s);
+    if (C <= 128) {
+      if (C == 32) hsel_warp_kernel<1><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
+      else if (C == 64) hsel_warp_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
+      else hsel_warp_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
+    } else {
+      int P = 64;
+      while (P < plan.cap || P < C) P <<= 1;
+      const size_t smem = (size_t)P * 8;
+      LSHG_CUDA(cudaFuncSetAttribute(hsel_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      hsel_block_kernel<<<nq, 512, smem, s>>>(cnt.ptr, cand.ptr, plan.cap, need, C, out, ovf.ptr);
+    }
+    count_launch();
+    LSHG_CHECK_LAUNCH();
+  }
+  // listed queries: exact popcount rescan written straight into their rows of `out`
+  launch_scan_bits_listed(xst, n, wp, words, qs, nq, op, C, ovf.ptr, out, s);
+}
+
+}  // namespace tc
+}  // namespace lshg

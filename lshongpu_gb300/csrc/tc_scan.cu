@@ -474,6 +474,21 @@ CUtensorMap make_map_e4m3(const void* base, int64_t rows, int box_rows) {
   return m;
 }
 
+CUtensorMap make_map_bytes(const void* base, int64_t rows, int kp, int box_rows) {
+  LSHG_REQUIRE(((uintptr_t)base & 15) == 0 && kp % 16 == 0 && kp >= 128, "TMA: 16-byte base and row stride");
+  LSHG_REQUIRE(box_rows >= 1 && box_rows <= 256, "TMA box rows must be in [1, 256]");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kp};
+  cuuint32_t box[2] = {128u, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(LSHG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
 namespace {
 
 template <int STAGES, int CT>

@@ -52,6 +52,33 @@ def test_same_alone_and_in_the_mix(engine, indexes):
     srv.close()
 
 
+@pytest.mark.parametrize("which", [0, 2, 3])
+def test_batching_window_coalesces_requests(engine, indexes, which):
+    """A burst of 40 requests (k from {10, 32, 100}) submitted within the 50 ms batching
+    window is answered in at most one launch a candidate class (exact scan and LSH: one;
+    tensor-core scan: k <= 32 and k > 32) -- far fewer launches than requests -- and every
+    request still equals its own query alone."""
+    x, idx = indexes
+    rng = np.random.default_rng(7)
+    srv = engine.Server(max_batch=4096, streams=2, use_graphs=True, batch_window_us=50_000)
+    srv.add_index(which, idx[which])
+    reqs = []
+    for t in range(40):
+        nq = int(rng.integers(1, 40))
+        k = int(rng.choice([10, 32, 100]))
+        q = datasets.clustered(nq, D, 2000 + t, count=50)
+        reqs.append((q, k))
+    tickets = [srv.submit(which, q, k) for q, k in reqs]
+    for (q, k), tk in zip(reqs, tickets):
+        out, _ = srv.wait(tk)
+        assert np.array_equal(out, idx[which].query(q, k))
+    st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["launches"] <= (2 if which == 3 else 1) + 2  # a burst split by the window at most once more
+    assert st["launches"] < len(reqs) // 4
+    srv.close()
+
+
 def test_admission_by_free_hbm(engine, indexes):
     _, idx = indexes
     srv = engine.Server(hbm_reserve_mb=1 << 30)  # more than any GPU has: everything refused
