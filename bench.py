@@ -178,8 +178,13 @@ def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
         return "tc_filter", "tensor8", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
     if path == "exact":
         return "scan_float", "fp32", 2.0 * nq * N_BASE * (d + PAD_DIM) / 1e12, "TFLOP/s"
-    # sketch scans are integer-bound at these batch sizes: work = sketch words compared
-    # (one XOR + POPC each, zero-byte count for byte samples), Q x N x words
+    # Hamming / one-bit Jaccard scans on the tensor cores: a +-1 E4M3 GEMM over the sketch
+    # bits, 2 x Q x N x bits FLOP, against the dense FP8 rate (2 x the measured bf16 figure)
+    if path in ("simhash", "wmh1") and "tc_hamming" in prof:
+        bits = 1024 if path == "simhash" else 256
+        return "tc_hamming", "tensor8", 2.0 * nq * N_BASE * bits / 1e12, "TFLOP/s"
+    # sketch scans on the popcount path are integer-bound at these batch sizes: work = sketch
+    # words compared (one XOR + POPC each, zero-byte count for byte samples), Q x N x words
     if path == "simhash":
         return "scan_bits", "popc", nq * N_BASE * 32 / 1e9, "Gword/s"
     if path == "wmh":
@@ -600,7 +605,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {"tc": "bf16", "tc8": "e4m3", "simhash": "u32", "wmh": "u8", "wmh1": "u32"}.get(args.path, "f32"),
+        "dtype": ({"tc": "bf16", "tc8": "e4m3", "wmh": "u8"}.get(args.path)
+              or ("e4m3 (+-1 sketch bits)" if "tc_hamming" in prof else None)
+              or {"simhash": "u32", "wmh1": "u32"}.get(args.path, "f32")),
         "data": "synthetic",
         "config": {"workload": workload_text(args), "global_batch": N_QUERY * world,
                    "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},

@@ -165,31 +165,37 @@ __global__ void __launch_bounds__(H_THREADS, 1)
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      int it = 0, ua = 0;
+      int it = 0, na = 0;  // base chunks and query tiles issued
       bool ok = true;
-      for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
+      for (int u = blockIdx.x; u < U && ok; u += gridDim.x) {
         const int qt = u % a.QT, c = u / a.QT;
         const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
-        // one query-tile buffer: the previous unit's MMAs must have completed
-        if (!mbar_wait(A_EMPTY, (ua & 1) ^ 1, abort_flag)) break;
-        mbar_expect_tx(A_FULL, LY::A_BYTES);
+        // The unit's first STAGES base chunks are issued before its query tile: their
+        // stages free up as the previous unit's MMAs consume the ring, so the copies run
+        // while those MMAs finish.  There is one query-tile buffer: it is reloaded once
+        // the previous unit's MMAs have completed.
+        const int total = (p1 - p0) * KC, pre = min(STAGES, total);
+        for (int ci = 0; ci <= total; ++ci) {
+          if (ci == pre) {
+            if (!mbar_wait(A_EMPTY, (na & 1) ^ 1, abort_flag)) { ok = false; break; }
+            mbar_expect_tx(A_FULL, LY::A_BYTES);
 #pragma unroll
-        for (int kc = 0; kc < KC; ++kc)
-          tma_load_2d(s0 + LY::A_OFF + kc * BM * H_CHUNK, &mapA, kc * H_CHUNK, qt * BM, A_FULL);
-        for (int p = p0; p < p1 && ok; ++p) {
-          const int row = p * a.dstride * HN;
-          for (int kc = 0; kc < KC; ++kc) {
-            const int st = it % STAGES, rd = it / STAGES;
-            if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
-            mbar_expect_tx(FULL(st), LY::B_BYTES);
-            tma_load_2d(s0 + LY::B_OFF + st * LY::B_BYTES, &mapB, kc * H_CHUNK, row, FULL(st));
-            ++it;
+            for (int kc = 0; kc < KC; ++kc)
+              tma_load_2d(s0 + LY::A_OFF + kc * BM * H_CHUNK, &mapA, kc * H_CHUNK, qt * BM, A_FULL);
+            ++na;
           }
+          if (ci == total) break;
+          const int p = p0 + ci / KC, kc = ci % KC;
+          const int st = it % STAGES, rd = it / STAGES;
+          if (!mbar_wait(EMPTY(st), (rd & 1) ^ 1, abort_flag)) { ok = false; break; }
+          mbar_expect_tx(FULL(st), LY::B_BYTES);
+          tma_load_2d(s0 + LY::B_OFF + st * LY::B_BYTES, &mapB, kc * H_CHUNK, p * a.dstride * HN, FULL(st));
+          ++it;
         }
       }
       // drain: every issued copy has landed before the CTA may exit
       for (int j = max(0, it - STAGES); j < it; ++j) mbar_wait(FULL(j % STAGES), (j / STAGES) & 1, abort_flag, true);
-      if (ua > 0) mbar_wait(A_FULL, (ua - 1) & 1, abort_flag, true);
+      if (na > 0) mbar_wait(A_FULL, (na - 1) & 1, abort_flag, true);
     }
     __syncwarp();
   } else if (warp == 1) {
