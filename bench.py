@@ -217,17 +217,18 @@ def dram_traffic(kernel: str, workload: str):
     return None
 
 
-def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7) -> dict:
+def serving_run(L, indexes: dict, rate_qps: float, seconds: float, truth=None, seed: int = 7,
+                window_us: int = 200, streams: int = 3) -> dict:
     """Open-loop Poisson arrivals of requests (batch size log-uniform in [1, 4096], k from
-    {10, 32, 100}, index type drawn uniformly) against the continuous-batching server;
-    latency = submit -> results on the host, as stamped by the library."""
+    {10, 32, 100}, index drawn uniformly) against the continuous-batching server;
+    latency = submit -> results on the host, as stamped by the library.  truth: (pool,
+    {index: (ids of the FP64 top-100 of the first rows of the pool)}) -- served rows of
+    those pool queries are scored for recall@k."""
     import threading
 
-    from lshongpu_gb300 import datasets
-
     rng = np.random.default_rng(seed)
-    pool = datasets.clustered(4096, DIM, seed=9001)
-    srv = L.Server(max_batch=4096, streams=3, use_graphs=True)
+    pool = truth[0] if truth else make_pool()
+    srv = L.Server(max_batch=4096, streams=streams, use_graphs=True, batch_window_us=window_us)
     for i, ix in indexes.items():
         srv.add_index(i, ix)
     ids = list(indexes)
@@ -241,48 +242,72 @@ def serving_run(L, indexes: dict, rate_qps: float, seconds: float, seed: int = 7
     st0 = srv.stats()
     mean_size = (4096 - 1) / np.log(4096.0)
     req_rate = rate_qps / mean_size
-    tickets, lat, sizes = [], [], []
+    nreq = max(1, int(req_rate * seconds))
+    gaps = rng.exponential(1.0 / req_rate, size=nreq)
+    sizes = np.exp(rng.uniform(0, np.log(4096), size=nreq)).astype(int)
+    ks = rng.choice([10, 32, 100], size=nreq)
+    which_i = rng.integers(0, len(ids), size=nreq)
+    offs = [int(rng.integers(0, 4096 - int(sz) + 1)) for sz in sizes]
+    tickets, lat = [], []
+    hits = {}  # index -> [matched, total]
     done = threading.Event()
+    tlim = truth[1] if truth else {}
 
     def waiter():
         i = 0
         while not (done.is_set() and i >= len(tickets)):
             if i < len(tickets):
-                _, l = srv.wait(tickets[i])
+                tk, which, off, sz, k = tickets[i]
+                out, l = srv.wait(tk)
                 lat.append(l / 1e3)
+                tid = tlim.get(which)
+                if tid is not None and off < len(tid):
+                    rows = range(off, min(off + sz, len(tid)))
+                    h = hits.setdefault(which, [0, 0])
+                    for r in rows:
+                        h[0] += len(set(out["ID"][r - off].tolist()) & set(tid[r][:k].tolist()))
+                        h[1] += k
                 i += 1
             else:
-                time.sleep(0.0005)
+                time.sleep(0.0002)
 
     th = threading.Thread(target=waiter)
     th.start()
     t0 = time.perf_counter()
     nxt = t0
-    while nxt - t0 < seconds:
-        now = time.perf_counter()
-        if now < nxt:
-            time.sleep(min(nxt - now, 0.002))
-            continue
-        size = int(np.exp(rng.uniform(0, np.log(4096))))
-        k = int(rng.choice([10, 32, 100]))
-        which = ids[int(rng.integers(0, len(ids)))]
-        off = int(rng.integers(0, 4096 - size + 1))
+    submitted = 0
+    for j in range(nreq):
+        nxt += gaps[j]
+        while time.perf_counter() < nxt:
+            pass
+        which, sz, k, off = ids[int(which_i[j])], int(sizes[j]), int(ks[j]), offs[j]
         try:
-            tickets.append(srv.submit(which, pool[off:off + size], k))
-            sizes.append(size)
+            tickets.append((srv.submit(which, pool[off:off + sz], k), which, off, sz, k))
+            submitted += sz
         except L.LshgError:
             pass  # refused by admission: counted in stats
-        nxt += rng.exponential(1.0 / req_rate)
     done.set()
     th.join()
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
     lat_a = np.array(lat)
-    return {"offered_qps": rate_qps, "achieved_qps": sum(sizes) / wall, "requests": len(tickets),
-            "p50_ms": float(np.percentile(lat_a, 50)), "p99_ms": float(np.percentile(lat_a, 99)),
-            "p999_ms": float(np.percentile(lat_a, 99.9)), "launches": st["launches"] - st0["launches"],
-            "graph_replays": st["graph_replays"] - st0["graph_replays"], "rejected": st["rejected"] - st0["rejected"]}
+    res = {"offered_qps": rate_qps, "achieved_qps": submitted / wall, "requests": len(tickets),
+           "p50_ms": float(np.percentile(lat_a, 50)), "p99_ms": float(np.percentile(lat_a, 99)),
+           "p999_ms": float(np.percentile(lat_a, 99.9)), "launches": st["launches"] - st0["launches"],
+           "graph_replays": st["graph_replays"] - st0["graph_replays"], "rejected": st["rejected"] - st0["rejected"],
+           "batch_window_us": window_us, "slots": streams}
+    res["launches_per_request"] = res["launches"] / max(1, res["requests"])
+    if hits:
+        res["recall_at_k"] = {str(w): h[0] / h[1] for w, h in hits.items() if h[1]}
+        res["recall_rows"] = {str(w): h[1] for w, h in hits.items()}
+    return res
+
+
+def make_pool():
+    from lshongpu_gb300 import datasets
+
+    return datasets.clustered(4096, DIM, seed=9001)
 
 
 def fp64_distances(x, q, ids, dist_fn):
@@ -590,16 +615,23 @@ def main():
                                       "sample": f"{nsub} queries x {N_BASE} points, FP32 SIMT exact scan"},
                 "ratio_value_over_simt": value / simt_qps}
             del simt
-        # serving: the same resident base behind the continuous-batching loop, mixed with
-        # a 1024-bit SimHash index and a cross-polytope LSH index (L=32, K=2) of it
+        # serving: the same resident base behind the continuous-batching loop, offered up
+        # to and past the batch capacity, then mixed with a 1024-bit SimHash index and a
+        # cross-polytope LSH index (L=32, K=2) of it; served rows of the first 256 pool
+        # queries are scored against the FP64 oracle's top-k
         if headline:
+            pool = make_pool()
+            t64, _ = oracle.fp64_topk(x, pool[:256], 100, threads=threads)
             serve_ix = {0: idx,
                         1: L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=1024)),
                         2: L.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7,
                                    bucketKeyBits=16, tables=32, options=L.make_options(cp_hashes=2))}
-            extras["serving"] = [serving_run(L, {0: idx}, rate, 3.0) for rate in (50_000, 200_000)]
-            extras["serving_mixed"] = serving_run(L, serve_ix, 20_000, 3.0)
-            extras["latency_ms"] = {k: extras["serving"][-1][k] for k in ("p50_ms", "p99_ms", "p999_ms")}
+            extras["serving"] = [serving_run(L, {0: idx}, rate, 2.0, truth=(pool, {0: t64}))
+                                 for rate in (500_000, 2_000_000, 4_000_000)]
+            extras["serving_mixed"] = serving_run(L, serve_ix, 300_000, 3.0, truth=(pool, {0: t64, 1: t64, 2: t64}))
+            best = max(extras["serving"], key=lambda r: r["achieved_qps"] if r["p99_ms"] < 50 else 0)
+            extras["latency_ms"] = {k: best[k] for k in ("p50_ms", "p99_ms", "p999_ms")}
+            extras["latency_ms"]["at_offered_qps"] = best["offered_qps"]
 
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,

@@ -279,7 +279,7 @@ Index::~Index() {
   x.release(); xnorm.release(); xt.release(); xs.release(); xse.release(); xsf.release(); xsft.release();
   sk_planes.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
-  xbf.release(); xbf_scale.release(); xf8.release(); xst.release(); qstats.release();
+  xbf.release(); xbf_scale.release(); xf8.release(); xnorm64.release(); xst.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();

@@ -78,6 +78,7 @@ struct Index {
   DevBuf<uint16_t> xbf;      // bf16 rows padded to dp
   DevBuf<float> xbf_scale;   // unused (kept for the file layout)
   DevBuf<uint8_t> xf8;       // E4M3 unit rows x kE4M3Scale, 128 bytes (implementation 9)
+  DevBuf<double> xnorm64;    // base row norms in double for the FP64 re-check (derived, not stored)
   int dp = 0;
 
   // Device error words of the query path (a pipeline or row-copy wait that timed out,
@@ -123,6 +124,9 @@ int next_pow2(int v);
 // Build idx.xst (the linear scans' tiled sketches) from idx.xs, and for Hamming / one-bit
 // Jaccard sketches of at most 1024 bits idx.xse (their E4M3 rows for the tensor cores).
 void tile_sketches(Index& idx, cudaStream_t stream);
+
+// Arrays derived from stored ones at build and at load: the tensor-core scans' FP64 row norms.
+void derive_tc(Index& idx, cudaStream_t stream);
 
 // Persistence (persist.cpp): checksummed binary image of a built index.
 void save_index(const Index& idx, const char* path);

@@ -91,7 +91,11 @@ void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t
 // and order each such run by the FP64 distance.
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d,
                    const float* xnorm, const float* q, const float* qnorm, int dist, int k,
-                   struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr, bool fp64_recheck = false);
+                   struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr, bool fp64_recheck = false,
+                   const double* xn64 = nullptr);
+// Row norms in double precision (sum of squares in dimension order, then sqrt): the FP64
+// re-check's base magnitudes.
+void launch_row_norms_fp64(const float* x, int64_t n, int d, double* out, cudaStream_t s);
 // The FP64 band of the re-rank: |FP32 distance - k-th| <= band_abs + band_rel * |k-th|.
 void fp64_band(int dist, int d, float* band_abs, float* band_rel);
 // Keys to result points (ID, distance); empty keys become (-1, INT_MAX).

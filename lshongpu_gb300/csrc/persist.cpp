@@ -403,7 +403,8 @@ std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
   upload_ops(I.ops_keys, s);
   upload_ops(I.ops_sketch, s);
   for (auto& kv : r.staged) kv.second.upload(s);
-  if (I.p.framework == 0 && I.xs.n) tile_sketches(I, s);  // derived layout, not stored
+  if (I.p.framework == 0 && I.xs.n) tile_sketches(I, s);  // derived layouts, not stored
+  if (I.p.framework == 0 && (I.p.implementation == 8 || I.p.implementation == 9)) derive_tc(I, s);
   I.qstats.alloc(2, s);
   LSHG_CUDA(cudaMemsetAsync(I.qstats.ptr, 0, I.qstats.bytes(), s));
   LSHG_CUDA(cudaStreamSynchronize(s));

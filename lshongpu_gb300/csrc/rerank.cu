@@ -27,33 +27,54 @@ namespace {
 
 constexpr int kBandMax = 256;  // entries a query's FP64 band re-scores at most
 
-// Double-precision distance of float rows, same definition as the FP32 formula: products
-// rounded, then added in dimension order (no fused multiply-add), as the FP64 CPU oracle.
+// Double-precision distance of float rows, same definition as the FP32 formula, computed
+// by a whole warp: lane l sums the terms of dimensions l, l + 32, ... in order (products of
+// floats are exact in double), then the 32 partial sums are added in a fixed tree to lane 0
+// and broadcast.  The GPU's FP64 pipe is narrow, and a warp instruction costs the same with
+// one active lane as with 32, so one lane walking a whole row would cost 32 times as much.
+// qq: the query's squared norm in double (angular only).
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+  return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// xn: the row's norm in double when the index keeps them (else computed here); qn: the
+// query's norm in double.
 template <int DIST>
-__device__ double fp64_distance(const float* __restrict__ xr, const float* qr, int d) {
+__device__ double fp64_distance_warp(const float* __restrict__ xr, const float* qr, int d, double qn, double xn,
+                                     int lane) {
   if (DIST == DIST_ANGULAR) {
-    double dot = 0.0, qq = 0.0, xx = 0.0;
-    for (int j = 0; j < d; ++j) {
-      const double a = qr[j], b = xr[j];
-      dot = __dadd_rn(dot, __dmul_rn(a, b));
-      qq = __dadd_rn(qq, __dmul_rn(a, a));
-      xx = __dadd_rn(xx, __dmul_rn(b, b));
+    double dot = 0.0, xx = 0.0;
+    if (xn > 0.0) {
+      for (int j = lane; j < d; j += 32) dot = __dadd_rn(dot, __dmul_rn((double)qr[j], (double)xr[j]));
+    } else {
+      for (int j = lane; j < d; j += 32) {
+        const double a = qr[j], b = xr[j];
+        dot = __dadd_rn(dot, __dmul_rn(a, b));
+        xx = __dadd_rn(xx, __dmul_rn(b, b));
+      }
+      xn = __dsqrt_rn(warp_sum_d(xx));
     }
-    return __dadd_rn(1.0, -__ddiv_rn(dot, __dmul_rn(__dsqrt_rn(qq), __dsqrt_rn(xx))));
+    dot = warp_sum_d(dot);
+    return __dadd_rn(1.0, -__ddiv_rn(dot, __dmul_rn(qn, xn)));
   } else if (DIST == DIST_JACCARD) {
     double mn = 0.0, mx = 0.0;
-    for (int j = 0; j < d; ++j) {
+    for (int j = lane; j < d; j += 32) {
       const double a = xr[j], b = qr[j];
       mn = __dadd_rn(mn, fmin(a, b));
       mx = __dadd_rn(mx, fmax(a, b));
     }
+    mn = warp_sum_d(mn);
+    mx = warp_sum_d(mx);
     return __dadd_rn(1.0, -__ddiv_rn(mn, mx));
   } else {
     double acc = 0.0;
-    for (int j = 0; j < d; ++j) {
+    for (int j = lane; j < d; j += 32) {
       const double df = __dadd_rn((double)qr[j], -(double)xr[j]);
       acc = __dadd_rn(acc, __dmul_rn(df, df));
     }
+    acc = warp_sum_d(acc);
     return DIST == DIST_EUCLID ? __dsqrt_rn(acc) : acc;
   }
 }
@@ -72,17 +93,23 @@ __device__ __forceinline__ uint64_t double_to_ordered(double v) {
 // searched among the first kBandMax entries.  Called by every thread of the block after
 // the sort; qr is the query row.
 template <int DIST>
-__device__ void fp64_runs(uint64_t* keys, int C, const float* __restrict__ x, int d, const float* qr, float band_abs,
-                          float band_rel) {
+__device__ void fp64_runs(uint64_t* keys, int C, int k, const float* __restrict__ x, const double* __restrict__ xn64,
+                          int d, const float* qr, float band_abs, float band_rel) {
   __shared__ uint64_t s_key[kBandMax];
   __shared__ uint64_t s_ord[kBandMax];
-  __shared__ short s_run[kBandMax];  // first entry of the entry's run
-  __shared__ short s_len[kBandMax];  // length of the entry's run
+  __shared__ short s_run[kBandMax];   // first entry of the entry's run
+  __shared__ short s_len[kBandMax];   // length of the entry's run
+  __shared__ short s_list[kBandMax];  // entries in runs of two or more
+  __shared__ int s_nlist;
+  __shared__ double s_qn;
   const int L = imin(C, kBandMax);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int i = threadIdx.x; i < L; i += blockDim.x) s_key[i] = keys[i];
   __syncthreads();
   if (threadIdx.x == 0) {
-    int start = 0;
+    // runs up to the one holding entry k - 1: only the first k entries are returned, and
+    // the runs before it decide them
+    int start = 0, nl = 0;
     for (int i = 1; i <= L; ++i) {
       bool join = false;
       if (i < L && s_key[i] != kEmptyKey && s_key[i - 1] != kEmptyKey) {
@@ -93,19 +120,34 @@ __device__ void fp64_runs(uint64_t* keys, int C, const float* __restrict__ x, in
         for (int j = start; j < i; ++j) {
           s_run[j] = (short)start;
           s_len[j] = (short)(i - start);
+          if (i - start > 1) s_list[nl++] = (short)j;
         }
         start = i;
+        if (i >= k) break;
       }
     }
+    s_nlist = nl;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < L; i += blockDim.x)
-    if (s_len[i] > 1) s_ord[i] = double_to_ordered(fp64_distance<DIST>(x + (int64_t)key_id(s_key[i]) * d, qr, d));
+  const int nl = s_nlist;
+  if (nl == 0) return;  // block-uniform
+  if (DIST == DIST_ANGULAR && warp == 0) {
+    double qq = 0.0;
+    for (int j = lane; j < d; j += 32) qq = __dadd_rn(qq, __dmul_rn((double)qr[j], (double)qr[j]));
+    qq = warp_sum_d(qq);
+    if (lane == 0) s_qn = __dsqrt_rn(qq);
+  }
   __syncthreads();
-  for (int i = threadIdx.x; i < L; i += blockDim.x) {
-    const int len = s_len[i];
-    if (len < 2) continue;
-    const int r0 = s_run[i];
+  for (int t = warp; t < nl; t += nwarps) {  // a warp a candidate
+    const int i = s_list[t];
+    const int id = key_id(s_key[i]);
+    const double v = fp64_distance_warp<DIST>(x + (int64_t)id * d, qr, d, s_qn, xn64 ? xn64[id] : 0.0, lane);
+    if (lane == 0) s_ord[i] = double_to_ordered(v);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nl; t += blockDim.x) {
+    const int i = s_list[t];
+    const int len = s_len[i], r0 = s_run[i];
     const uint64_t oi = s_ord[i];
     const uint32_t ii = (uint32_t)key_id(s_key[i]);
     int r = 0;
@@ -143,7 +185,7 @@ template <int DIST>
 __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                               int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
                               const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, float band_abs,
-                              float band_rel) {
+                              float band_rel, const double* __restrict__ xn64) {
   extern __shared__ __align__(16) unsigned char rsm[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(rsm);
   float* qr = reinterpret_cast<float*>(rsm + (size_t)C * 8);
@@ -165,7 +207,7 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, x, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -184,7 +226,7 @@ template <int DIST>
 __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                                      int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
                                      const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, int* err,
-                                     float band_abs, float band_rel) {
+                                     float band_abs, float band_rel, const double* __restrict__ xn64) {
   extern __shared__ __align__(128) unsigned char rsm[];
   const int CH = blockDim.x;
   const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
@@ -246,7 +288,7 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, x, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
   for (int i = tid; i < k; i += CH) {
     const uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -304,7 +346,7 @@ void fp64_band(int dist, int d, float* band_abs, float* band_rel) {
 
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d, const float* xnorm,
                    const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s, int* err,
-                   bool fp64_recheck) {
+                   bool fp64_recheck, const double* xn64) {
   if (nq <= 0) return;
   float band_abs = -1.0f, band_rel = 0.0f;
   if (fp64_recheck) fp64_band(dist, d, &band_abs, &band_rel);
@@ -319,7 +361,7 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
     LSHG_CUDA(cudaFuncSetAttribute(rerank_staged_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                    (int)staged_smem));                                                         \
     rerank_staged_kernel<DV><<<nq, CH, staged_smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, err, \
-                                                         band_abs, band_rel);                                \
+                                                         band_abs, band_rel, xn64);                          \
   } while (0)
     switch (dist) {
       case DIST_ANGULAR: LSHG_RRS(DIST_ANGULAR); break;
@@ -340,7 +382,7 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
   do {                                                                                                    \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
     rerank_kernel<DV><<<nq, threads, smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, band_abs,   \
-                                                band_rel);                                                \
+                                                band_rel, xn64);                                          \
   } while (0)
   switch (dist) {
     case DIST_ANGULAR: LSHG_RR(DIST_ANGULAR); break;
@@ -350,6 +392,25 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
     default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "re-rank: invalid distance function");
   }
 #undef LSHG_RR
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+__global__ void row_norms_fp64_kernel(const float* __restrict__ x, int64_t n, int d, double* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double ss = 0.0;
+    for (int j = 0; j < d; ++j) {
+      const double v = x[i * d + j];
+      ss = __dadd_rn(ss, __dmul_rn(v, v));
+    }
+    out[i] = __dsqrt_rn(ss);
+  }
+}
+
+void launch_row_norms_fp64(const float* x, int64_t n, int d, double* out, cudaStream_t s) {
+  if (n <= 0) return;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8);
+  row_norms_fp64_kernel<<<blocks, 256, 0, s>>>(x, n, d, out);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }

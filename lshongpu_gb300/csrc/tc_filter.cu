@@ -461,15 +461,16 @@ __global__ void __launch_bounds__(256) tau_select_reg_kernel(const float* __rest
 // queries whose survivors overflowed the candidate array (ovf[0] = count, ovf[1..] = ids).
 template <int E>
 __global__ void __launch_bounds__(256) cand_select_kernel(const int* __restrict__ cnt,
-                                                           const uint64_t* __restrict__ cand, int cap, int nq,
-                                                           uint64_t* __restrict__ out, int* __restrict__ ovf) {
+                                                           const uint64_t* __restrict__ cand, int cap, int need,
+                                                           int nq, uint64_t* __restrict__ out,
+                                                           int* __restrict__ ovf) {
   constexpr int CT = 32 * E;
   const int lane = threadIdx.x & 31;
   const int q = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (q >= nq) return;  // warp-uniform
   const int c = cnt[q];
   uint64_t* dst = out + (int64_t)q * CT;
-  if (c > cap) {
+  if (c > cap || c < need) {
 #pragma unroll
     for (int e = 0; e < E; ++e) dst[e * 32 + lane] = kEmptyKey;
     if (lane == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
@@ -569,19 +570,34 @@ void run_filter(const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap&
 
 }  // namespace
 
-// Prepass parameters in units of TN-point tiles.  The target is M (group maxima a row)
-// of at least 4 CT, so that the CT-th largest maximum is a tight bound, and a sample of
-// at most 1/8 of the base; survivors then number about CT * S a query.
+// Prepass parameters in units of TN-point tiles.  Large bases sample every S-th tile
+// (S <= 16) and take tau at rank r = CT/S + 4 sqrt(CT/S) + 8 of the sample's 64-column
+// maxima: the query's CT-th best point puts about CT/S points of the sample above it, so
+// tau stays at or below that point unless the count exceeds its mean by four standard
+// deviations, and about r * S points survive (CT * S with r = CT).  A query with fewer
+// than CT survivors is rescanned exactly by the list kernel (cand_select lists it), so
+// the rank only trades survivors against fallbacks.  S is the largest that leaves at
+// least 4 r maxima a row, so that the r-th largest is a tight bound.
 FilterPlan plan_filter(int64_t n, int CT) {
   FilterPlan p{};
   const int NT = ceil_div(n, TN);
   p.NT = NT;
+  p.rank = CT;
   if (NT >= CT) {  // 64-column maxima: 4 a tile
     p.GW = 64;
-    p.S = (int)std::max<int64_t>(1, std::min<int64_t>(8, NT / (4 * CT)));
+    p.S = 1;
+    for (int S : {16, 8, 4, 2}) {
+      const double m = (double)CT / S;
+      const int r = std::min(CT, (int)std::ceil(m + 4.0 * std::sqrt(m) + 8.0));
+      if (4 * ceil_div(NT, S) >= 4 * r) {
+        p.S = S;
+        p.rank = r;
+        break;
+      }
+    }
     p.NS = ceil_div(NT, p.S);
     p.M = 4 * p.NS;
-    p.cap = std::max(1024, 4 * CT * p.S);
+    p.cap = std::max(1024, 4 * p.rank * p.S);
   } else if (NT * 32 >= 4 * CT) {  // 8-column maxima: 32 a tile
     p.GW = 8;
     p.S = 1;
@@ -624,7 +640,7 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
       if (plan.GW == 64) run_filter<MODE_GROUPMAX, 64, false>(ma, mb, mbhi, a, "tc_prepass", s);
       else run_filter<MODE_GROUPMAX, 8, false>(ma, mb, mbhi, a, "tc_prepass", s);
     }
-    launch_tau_select(gmax.ptr, nq, plan.M, CT, margin, tau, s);
+    launch_tau_select(gmax.ptr, nq, plan.M, plan.rank, margin, tau, s);
   }
   a.gmax = nullptr;
   a.M = 0;
@@ -648,12 +664,12 @@ void launch_tau_select(const float* gmax, int nq, int M, int rank, float margin,
   LSHG_CHECK_LAUNCH();
 }
 
-void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
-                        cudaStream_t s) {
+void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int need, int CT, uint64_t* out,
+                        int* ovf, cudaStream_t s) {
   ProfScope _ps("tc_cand_select", s);
-  if (CT == 32) cand_select_kernel<1><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
-  else if (CT == 64) cand_select_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
-  else if (CT == 128) cand_select_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, nq, out, ovf);
+  if (CT == 32) cand_select_kernel<1><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, need, nq, out, ovf);
+  else if (CT == 64) cand_select_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, need, nq, out, ovf);
+  else if (CT == 128) cand_select_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, need, nq, out, ovf);
   else throw Error(LSHG_ERR_INVALID_ARGUMENT, "tensor-core scan: candidate count must be 32, 64 or 128");
   count_launch();
   LSHG_CHECK_LAUNCH();

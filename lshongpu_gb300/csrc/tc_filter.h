@@ -24,6 +24,7 @@ struct FilterPlan {
   int S;    // prepass samples every S-th base tile
   int NS;   // sampled tiles
   int M;    // group maxima a query row
+  int rank; // tau = the rank-th largest group maximum (CT, or fewer with sampling: see plan_filter)
   int cap;  // survivor slots a query
 };
 
@@ -42,10 +43,10 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
 // row's M group maxima, minus margin; -inf when the row holds fewer than rank maxima.
 void launch_tau_select(const float* gmax, int nq, int M, int rank, float margin, float* tau, cudaStream_t s);
 
-// Top-CT keys a query from its survivors (CT = 32, 64 or 128); overflowed queries are
-// listed in ovf.
-void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int CT, uint64_t* out, int* ovf,
-                        cudaStream_t s);
+// Top-CT keys a query from its survivors (CT = 32, 64 or 128); queries with more survivors
+// than cap or fewer than `need` are listed in ovf for the exact fallback.
+void launch_cand_select(const int* cnt, const uint64_t* cand, int nq, int cap, int need, int CT, uint64_t* out,
+                        int* ovf, cudaStream_t s);
 
 // Tensor-core sketch scan (tc_hamming.cu): threshold plan for a base of n points and the
 // top-C of each query.  ok = false: no prepass shape bounds C well (use the popcount scan).

@@ -23,7 +23,9 @@
 //   filter   on the whole base keeps the points whose score reaches tau[q], staged per row
 //            in shared memory and moved to the query's candidate array with one atomicAdd
 //            a batch;
-//   select   sorts each query's survivors by (score desc, id asc) and keeps the first C.
+//   select   keeps each query's first C survivors by (score desc, id asc): a warp sort for
+//            C <= 128, a histogram of the integer scores and a sort of the ties at the
+//            C-th score beyond.
 //            A query with fewer than C survivors (tau above its C-th best score: the
 //            sample was unrepresentative) or more than its array holds (massive ties) is
 //            listed and rescanned exactly by the popcount scan on the device, so the result
@@ -103,14 +105,12 @@ struct HArgs {
   int* err;
 };
 
-__device__ __forceinline__ void h_flush(int* cnt, uint64_t* dst, int cap, const float* ssc, const int* sid,
-                                        int& scnt) {
-  if (scnt > 0) {
-    const int base = atomicAdd(cnt, scnt);
-    for (int e = 0; e < scnt; ++e)
-      if (base + e < cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
-    scnt = 0;
-  }
+// Out of line: called from every group of the unrolled survivor path, inlined copies would
+// crowd the instruction cache.
+__device__ __noinline__ void h_flush(int* cnt, uint64_t* dst, int cap, const float* ssc, const int* sid, int scnt) {
+  const int base = atomicAdd(cnt, scnt);
+  for (int e = 0; e < scnt; ++e)
+    if (base + e < cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
 }
 
 template <int MODE, int GW, int KC>
@@ -310,13 +310,16 @@ __global__ void __launch_bounds__(H_THREADS, 1)
                 int ng = 0;
 #pragma unroll
                 for (int jj = 0; jj < 8; ++jj) ng += __uint_as_float(v[8 * gg + jj]) >= tau ? 1 : 0;
-                if (scnt + ng > SBUF) h_flush(qcnt, qdst, a.cap, ssc, sid, scnt);
+                if (scnt + ng > SBUF) {
+                  h_flush(qcnt, qdst, a.cap, ssc, sid, scnt);
+                  scnt = 0;
+                }
               }
 #pragma unroll
               for (int jj = 0; jj < 8; ++jj) {
                 const float sc = __uint_as_float(v[8 * gg + jj]);
                 if (sc >= tau) {
-                  if (SBUF > 0 && scnt < SBUF) {
+                  if (SBUF >= 8 || (SBUF > 0 && scnt < SBUF)) {  // 8 entries always fit after a flush
                     ssc[scnt * BM] = sc;
                     sid[scnt * BM] = ibase + 8 * gg + jj;
                     ++scnt;
@@ -330,8 +333,10 @@ __global__ void __launch_bounds__(H_THREADS, 1)
           }
         }
       }
-      if (MODE == MODE_FILTER && SBUF > 0 && scnt > 0)  // the next unit is another query tile
+      if (MODE == MODE_FILTER && SBUF > 0 && scnt > 0) {  // the next unit is another query tile
         h_flush(a.cnt + q, a.cand + (int64_t)q * a.cap, a.cap, ssc, sid, scnt);
+        scnt = 0;
+      }
     }
   }
 
@@ -411,25 +416,88 @@ __global__ void __launch_bounds__(256) hsel_warp_kernel(const int* __restrict__ 
   for (int e = 0; e < E; ++e) dst[e * 32 + lane] = best[e];
 }
 
-// Top-C (C > 128) of each query's survivors, one block a query: the survivors (at most
-// cap <= H_SEL_MAX) sorted in shared memory, the first C written.  Same listing rule.
-__global__ void __launch_bounds__(512) hsel_block_kernel(const int* __restrict__ cnt,
-                                                         const uint64_t* __restrict__ cand, int cap, int need, int C,
-                                                         uint64_t* __restrict__ out, int* __restrict__ ovf) {
-  extern __shared__ uint64_t keys[];
-  const int q = blockIdx.x;
+// Top-C (C > 128) of each query's survivors as a set, one block a query, using the integer
+// scores: a histogram of the scores (2 * bits + 1 bins) gives the score t of the C-th best
+// survivor; every survivor above t is in, and of those at t the ones with the lowest ids
+// (the survivors' keys sorted in shared memory: they order by id within one score).  The
+// set goes out unordered -- the re-rank sorts it.  A query whose survivors at t exceed
+// H_TIE_MAX is listed for the exact rescan, as are those with fewer than `need` or more
+// than `cap` survivors.
+constexpr int H_TIE_MAX = 4096;
+constexpr int H_BINS_MAX = 2049;
+
+__global__ void __launch_bounds__(512) hsel_hist_kernel(const int* __restrict__ cnt, const uint64_t* __restrict__ cand,
+                                                        int cap, int need, int C, int bits,
+                                                        uint64_t* __restrict__ out, int* __restrict__ ovf) {
+  __shared__ uint64_t tie[H_TIE_MAX];
+  __shared__ int hist[H_BINS_MAX];
+  __shared__ int s_t, s_below, s_nout, s_ntie;
+  const int q = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
   const int c = cnt[q];
   if (c > cap || c < need) {
-    if (threadIdx.x == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
+    if (tid == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
     return;
   }
-  int P = 64;
-  while (P < c || P < C) P <<= 1;
   const uint64_t* src = cand + (int64_t)q * cap;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) keys[i] = i < c ? src[i] : kEmptyKey;
+  uint64_t* dst = out + (int64_t)q * C;
+  if (c <= C) {  // a base of fewer than C points: all of them, then empty keys
+    for (int i = tid; i < C; i += blockDim.x) dst[i] = i < c ? src[i] : kEmptyKey;
+    return;
+  }
+  const int nb = 2 * bits + 1;
+  for (int i = tid; i < nb; i += blockDim.x) hist[i] = 0;
+  if (tid == 0) {
+    s_nout = 0;
+    s_ntie = 0;
+  }
   __syncthreads();
-  block_bitonic_sort(keys, P);
-  for (int i = threadIdx.x; i < C; i += blockDim.x) out[(int64_t)q * C + i] = keys[i];
+  // a key holds -score; bin = bits - score: 0 is the best score
+  for (int i = tid; i < c; i += blockDim.x) atomicAdd(&hist[(int)key_dist(src[i]) + bits], 1);
+  __syncthreads();
+  if (tid < 32) {  // the bin where the running count reaches C
+    const int per = (nb + 31) / 32, b0 = lane * per, b1 = min(nb, b0 + per);
+    int own = 0;
+    for (int b = b0; b < b1; ++b) own += hist[b];
+    int incl = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const unsigned hit = __ballot_sync(0xffffffffu, incl >= C);
+    const int L = __ffs(hit) - 1;  // hit != 0: the bins hold c > C keys
+    if (lane == L) {
+      int acc = incl - own;
+      for (int b = b0; b < b1; ++b) {
+        if (acc + hist[b] >= C) {
+          s_t = b;
+          s_below = acc;
+          break;
+        }
+        acc += hist[b];
+      }
+    }
+  }
+  __syncthreads();
+  const int t = s_t, below = s_below;
+  const int nt = hist[t];
+  if (nt > H_TIE_MAX) {  // block-uniform
+    if (tid == 0) ovf[1 + atomicAdd(ovf, 1)] = q;
+    return;
+  }
+  for (int i = tid; i < c; i += blockDim.x) {
+    const uint64_t key = src[i];
+    const int b = (int)key_dist(key) + bits;
+    if (b < t) dst[atomicAdd(&s_nout, 1)] = key;
+    else if (b == t) tie[atomicAdd(&s_ntie, 1)] = key;
+  }
+  __syncthreads();
+  int P = 64;
+  while (P < nt) P <<= 1;
+  for (int i = nt + tid; i < P; i += blockDim.x) tie[i] = kEmptyKey;
+  __syncthreads();
+  block_bitonic_sort(tie, P);
+  for (int i = tid; i < C - below; i += blockDim.x) dst[below + i] = tie[i];
 }
 
 // Rows of kp bytes (a multiple of 128); boxes of 128 bytes x box_rows rows, 128-byte swizzle.
@@ -584,11 +652,7 @@ void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int w
       else if (C == 64) hsel_warp_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
       else hsel_warp_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
     } else {
-      int P = 64;
-      while (P < plan.cap || P < C) P <<= 1;
-      const size_t smem = (size_t)P * 8;
-      LSHG_CUDA(cudaFuncSetAttribute(hsel_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      hsel_block_kernel<<<nq, 512, smem, s>>>(cnt.ptr, cand.ptr, plan.cap, need, C, out, ovf.ptr);
+      hsel_hist_kernel<<<nq, 512, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, C, 32 * words, out, ovf.ptr);
     }
     count_launch();
     LSHG_CHECK_LAUNCH();

@@ -517,6 +517,13 @@ void tc_prepare(Index& I, cudaStream_t s) {
     I.xf8.alloc((size_t)npad * KD, s);
     to_unit_e4m3(I.x.ptr, I.n, I.d, npad, I.xf8.ptr, s);
   }
+  derive_tc(I, s);
+}
+
+void derive_tc(Index& I, cudaStream_t s) {
+  if (I.p.opt.fp64_recheck == 0) return;
+  I.xnorm64.alloc((size_t)I.n, s);
+  launch_row_norms_fp64(I.x.ptr, I.n, I.d, I.xnorm64.ptr, s);
 }
 
 void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
@@ -569,10 +576,12 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
 
   // 3. top-CT of the survivors
   DevBuf<uint64_t> best((size_t)nq * CT, s);
-  launch_cand_select(cnt.ptr, cand.ptr, nq, plan.cap, CT, best.ptr, ovf, s);
+  // a query needs min(CT, n) survivors: fewer means its sampled threshold was too high
+  launch_cand_select(cnt.ptr, cand.ptr, nq, plan.cap, (int)std::min<int64_t>(CT, I.n), CT, best.ptr, ovf, s);
 
-  // 4. overflow fallback (a query can only overflow when it has more survivors than slots)
-  if ((int64_t)plan.cap < I.n) {
+  // 4. fallback for queries with more survivors than slots (massive ties) or fewer than CT
+  //    (a sampled threshold above the query's CT-th best score)
+  if ((int64_t)plan.cap < I.n || plan.rank < CT) {
     ProfScope _ps("tc_fallback", s);
     const int G = num_sms();
     DevBuf<uint16_t> qg((size_t)qpad * KD, s);
@@ -588,7 +597,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   DevBuf<float> qn((size_t)nq, s);
   launch_row_norms(q, nq, I.d, qn.ptr, s);
   launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s, err,
-                I.p.opt.fp64_recheck != 0);
+                I.p.opt.fp64_recheck != 0, I.xnorm64.ptr);
 }
 
 }  // namespace lshg
