@@ -19,7 +19,8 @@ prints its own line with its own metric; the headline is the default):
   3       tensor-core exact scan, N = 1M, d = 128 (100 + 28 zero dims), Q = 16,384 (3-fp8:
           E4M3 tensor-core scores; --path tc8 runs E4M3 at any size)
   4a      cross-polytope LSH, L = 32 tables, K = 2 hashes a key, 3 rounds, N = 1M, d = 128
-          padded, Q = 10k, exact angular distance on candidates (4a-k1: K = 1)
+          padded, Q = 10k, exact angular distance on candidates (4a-k1: K = 1; 4a-l48: L = 48,
+          the table count that reaches recall@32 >= 0.99)
   4b      weighted MinHash, 256 byte samples, N = 500k, d = 100 sparse Gamma(2,1) values
           (30% nonzero), Q = 10k, Jaccard sketch scan + generalized-Jaccard re-rank
           (4b-1bit: 256 one-bit samples)
@@ -55,6 +56,7 @@ PAD_DIM = 0        # zero dimensions appended to every vector
 DATA = "clustered"  # or "sparse" (weighted MinHash configuration)
 CAND = 1024         # SimHash candidates re-ranked
 CP_HASHES = 2       # cross-polytope hashes a key
+CP_TABLES = 32      # LSH tables
 
 # measurement configurations: path and shape overrides
 CONFIGS = {
@@ -65,6 +67,7 @@ CONFIGS = {
     "3-fp8": dict(path="tc8", N_BASE=1_000_000, N_QUERY=16_384, PAD_DIM=28),
     "4a": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=2),
     "4a-k1": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=1),
+    "4a-l48": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=2, CP_TABLES=48),
     "4b": dict(path="wmh", N_BASE=500_000, DATA="sparse"),
     "4b-1bit": dict(path="wmh1", N_BASE=500_000, DATA="sparse"),
 }
@@ -152,7 +155,7 @@ def build_index(L, x, path: str):
         return L.Index(x, implementation=3, sketchDim=32, options=L.make_options(candidates=CAND))
     if path == "cplsh":
         return L.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7,
-                       bucketKeyBits=8 * CP_HASHES, tables=32, options=L.make_options(cp_hashes=CP_HASHES))
+                       bucketKeyBits=8 * CP_HASHES, tables=CP_TABLES, options=L.make_options(cp_hashes=CP_HASHES))
     if path == "wmh":
         return L.Index(x, implementation=4, distanceFunc=2, sketchDim=256)
     if path == "wmh1":
@@ -335,7 +338,7 @@ def workload_text(args) -> str:
     what = {"tc": "tensor-core exact scan", "tc8": "tensor-core exact scan, E4M3 (FP8) scores",
             "exact": "FP32 SIMT exact scan",
             "simhash": f"1024-bit SimHash, {CAND} candidates re-ranked",
-            "cplsh": f"cross-polytope LSH, L=32, K={CP_HASHES}, 3 rounds, exact angular on candidates",
+            "cplsh": f"cross-polytope LSH, L={CP_TABLES}, K={CP_HASHES}, 3 rounds, exact angular on candidates",
             "wmh": "weighted MinHash, 256 byte samples, Jaccard scan + generalized-Jaccard re-rank",
             "wmh1": "weighted MinHash, 256 one-bit samples, Jaccard scan + generalized-Jaccard re-rank"}[args.path]
     cfg = f"configuration {args.config}: " if args.config else ""
@@ -388,6 +391,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
     ap.add_argument("--n", type=int, default=None, help="base size (profiling cases only)")
     ap.add_argument("--nq", type=int, default=None, help="queries per step (profiling cases only)")
+    ap.add_argument("--tables", type=int, default=None, help="LSH tables (cross-polytope configurations)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.config:
@@ -401,6 +405,8 @@ def main():
         globals()["N_BASE"] = args.n
     if args.nq is not None:
         globals()["N_QUERY"] = args.nq
+    if args.tables is not None:
+        globals()["CP_TABLES"] = args.tables
     args.path = args.path or "tc"
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

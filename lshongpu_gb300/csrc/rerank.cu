@@ -226,17 +226,24 @@ template <int DIST>
 __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                                      int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
                                      const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, int* err,
-                                     float band_abs, float band_rel, const double* __restrict__ xn64) {
+                                     float band_abs, float band_rel, const double* __restrict__ xn64, int test_stall) {
   extern __shared__ __align__(128) unsigned char rsm[];
   const int CH = blockDim.x;
   const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
   unsigned char* stage = rsm;
   uint64_t* keys = reinterpret_cast<uint64_t*>(rsm + (size_t)CH * slot);
   float* qr = reinterpret_cast<float*>(keys + C);
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bar, never;
   const int qi = blockIdx.x, tid = threadIdx.x;
   const uint32_t bar_a = tc::smem_u32(&bar);
-  if (tid == 0) tc::mbar_init(bar_a, 1);
+  // test_stall: the first wait is made on `never`, a barrier nothing arrives on, with a
+  // 1 ms limit -- the give-up path (error 3, rows read directly, the copy drained at exit)
+  // runs without any fault
+  const uint32_t never_a = tc::smem_u32(&never);
+  if (tid == 0) {
+    tc::mbar_init(bar_a, 1);
+    tc::mbar_init(never_a, 1);
+  }
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
   __syncthreads();
@@ -261,11 +268,14 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
       if (tid == 0) tc::mbar_expect_tx(bar_a, (uint32_t)nv * rowb);
       __syncthreads();
       if (id >= 0) tc::bulk_load(tc::smem_u32(dst), x + (int64_t)id * d, rowb, bar_a);
-      bool got = tc::mbar_try(bar_a, phase);
+      const bool stall = test_stall && c0 == 0;
+      const uint32_t wbar = stall ? never_a : bar_a;
+      const uint64_t limit = stall ? 1000000ull : tc::kWaitNs;
+      bool got = tc::mbar_try(wbar, phase);
       if (!got) {
         const uint64_t t0 = tc::global_ns();
-        while (!(got = tc::mbar_try_sleep(bar_a, phase, 20000u)))
-          if (tc::global_ns() - t0 > tc::kWaitNs) break;
+        while (!(got = tc::mbar_try_sleep(wbar, phase, 20000u)))
+          if (tc::global_ns() - t0 > limit) break;
       }
       ok = __syncthreads_and(got);
       if (!ok) {
@@ -350,6 +360,10 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
   if (nq <= 0) return;
   float band_abs = -1.0f, band_rel = 0.0f;
   if (fp64_recheck) fp64_band(dist, d, &band_abs, &band_rel);
+  // test hook: LSHG_TEST_ROW_WAIT_STALL=1 makes the first row-copy wait of the staged
+  // re-rank run out (see rerank_staged_kernel)
+  const char* stall_env = getenv("LSHG_TEST_ROW_WAIT_STALL");
+  const int test_stall = (stall_env && stall_env[0] == '1') ? 1 : 0;
   LSHG_REQUIRE((C & (C - 1)) == 0 && C >= 2, "re-rank: candidate count must be a power of two");
   ProfScope _ps("rerank", s);
   // staged: rows of d % 4 == 0 floats, 16-byte aligned, up to 128 a chunk
@@ -361,7 +375,7 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
     LSHG_CUDA(cudaFuncSetAttribute(rerank_staged_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                    (int)staged_smem));                                                         \
     rerank_staged_kernel<DV><<<nq, CH, staged_smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, err, \
-                                                         band_abs, band_rel, xn64);                          \
+                                                         band_abs, band_rel, xn64, test_stall);              \
   } while (0)
     switch (dist) {
       case DIST_ANGULAR: LSHG_RRS(DIST_ANGULAR); break;

@@ -59,12 +59,13 @@ struct Request {
 };
 
 // Requests whose (index, class) match get the same candidates whatever their k, so they
-// can share a launch run at the largest k.  Tensor-core scans re-rank 64 candidates for
-// k <= 32 and 128 beyond; sketched scans max(C, k rounded up); exact scans and LSH
+// can share a launch run at the largest k.  The BF16 tensor-core scan re-ranks 64
+// candidates for k <= 32 and 128 beyond, the E4M3 one 128 always; sketched scans max(C, k rounded up); exact scans and LSH
 // buckets do not depend on k.
 int batch_class(const Index& I, int k) {
   const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
-  if (I.p.framework == 0 && (impl == 8 || impl == 9)) return k <= 32 ? 0 : 1;
+  if (I.p.framework == 0 && impl == 8) return k <= 32 ? 0 : 1;
+  if (I.p.framework == 0 && impl == 9) return 0;  // 128 candidates at every k
   int kp = 32;
   while (kp < k) kp <<= 1;
   const bool sketched = I.p.framework == 0 ? (impl >= 3 && impl <= 6) : (I.p.runWithSketchedData && I.sk_kind);

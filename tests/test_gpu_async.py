@@ -110,3 +110,30 @@ def test_device_error_reported_on_its_own_stream(engine):
     got = ob.cpu().numpy()
     assert np.array_equal(got[:, :, 0], ref["ID"])
     assert np.array_equal(got[:, :, 1].view(np.float32), ref["distance"])
+
+
+def test_row_copy_wait_gives_up_with_timeout_status(engine, monkeypatch):
+    """The re-rank's first row-copy wait is made to run out (test hook: it waits on a
+    barrier nothing arrives on, for 1 ms): the kernel raises LSHG_ERR_TIMEOUT on the
+    stream's error word, reads the rows directly instead, waits for its copy in flight
+    before it exits, and the results equal the staged read's.  The index stays usable."""
+    import torch
+
+    x = datasets.clustered(20000, D, 161, count=40)
+    q = datasets.clustered(200, D, 162, count=40)
+    idx = engine.Index(x, implementation=engine.IMPL_TC, distanceFunc=1)
+    ref = idx.query(q, 32)
+    dq = torch.from_numpy(q).cuda()
+    out = torch.full((200, 32, 2), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    monkeypatch.setenv("LSHG_TEST_ROW_WAIT_STALL", "1")
+    idx.query_device_async(dq.data_ptr(), 200, 32, out.data_ptr())
+    with pytest.raises(engine.LshgError) as e:
+        idx.sync()
+    assert e.value.status == 8  # LSHG_ERR_TIMEOUT
+    monkeypatch.delenv("LSHG_TEST_ROW_WAIT_STALL")
+    got = out.cpu().numpy()
+    assert np.array_equal(got[:, :, 0], ref["ID"])
+    assert np.array_equal(got[:, :, 1].view(np.float32), ref["distance"])
+    idx.sync()  # reported once
+    assert np.array_equal(idx.query(q, 32), ref)

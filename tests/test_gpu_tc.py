@@ -155,10 +155,11 @@ def test_tc_edge_shapes(engine, orc, n, nq, k, d):
 
 
 # ---- E4M3 (FP8) tensor-core scores (implementation 9) ------------------------------------
-# Tolerance stated: recall@k >= 0.98 against the exact FP32 scan (E4M3 keeps 3 mantissa
+# Tolerance stated: recall@k >= 0.99 against the exact FP32 scan (E4M3 keeps 3 mantissa
 # bits, so more near-equal neighbours trade places at the candidate boundary than with
-# BF16; 128 candidates are re-ranked a query), and every returned distance equals the
-# oracle's FP32 distance for that id bit for bit (the re-rank is the same FP32 code).
+# BF16; 128 candidates are re-ranked a query at every k), and every returned distance
+# equals the oracle's FP32 distance for that id bit for bit (the re-rank is the same FP32
+# code).
 
 
 @pytest.mark.parametrize("n,nq,k,d", [(1000, 200, 32, 100), (20000, 300, 32, 100), (6000, 129, 100, 100),
@@ -171,7 +172,7 @@ def test_tc_fp8_recall_and_exact_distances(engine, orc, n, nq, k, d):
     kk = min(k, n)
     ids, ds = orc.exact_topk(x, q, kk, dist=1)
     rec = recall(res["ID"][:, :kk], ids)
-    assert rec >= 0.98, f"E4M3 recall@{kk} = {rec:.4f}"
+    assert rec >= 0.99, f"E4M3 recall@{kk} = {rec:.4f}"
     lookup = [dict(zip(i.tolist(), dd.tolist())) for i, dd in zip(ids, ds)]
     for qi in range(nq):
         for rid, rd in zip(res["ID"][qi], res["distance"][qi]):
@@ -194,7 +195,7 @@ def test_tc_fp8_overflow_and_persistence(engine, orc, tmp_path):
     ids, ds = orc.exact_topk(x, q, 32, dist=1)
     assert res["ID"][5].tolist() == ids[5].tolist()
     assert np.array_equal(res["distance"][5], ds[5])
-    assert recall(res["ID"], ids) >= 0.98
+    assert recall(res["ID"], ids) >= 0.99
     p = str(tmp_path / "fp8.idx")
     idx.save(p)
     again = engine.Index.load(p).query(q, 32)
