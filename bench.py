@@ -144,11 +144,16 @@ def make_data(seed_offset: int):
     return x, q
 
 
+FP64_RECHECK = -1  # lshg_options.fp64_recheck of the benchmarked index
+
+
 def build_index(L, x, path: str):
     if path == "tc":
-        return L.Index(x, implementation=L.IMPL_TC, distanceFunc=1, options=L.make_options(candidates=64))
+        return L.Index(x, implementation=L.IMPL_TC, distanceFunc=1,
+                       options=L.make_options(candidates=64, fp64_recheck=FP64_RECHECK))
     if path == "tc8":
-        return L.Index(x, implementation=L.IMPL_TC_FP8, distanceFunc=1)
+        return L.Index(x, implementation=L.IMPL_TC_FP8, distanceFunc=1,
+                       options=L.make_options(fp64_recheck=FP64_RECHECK))
     if path == "exact":
         return L.Index(x, implementation=2, distanceFunc=1)
     if path == "simhash":
@@ -392,6 +397,8 @@ def main():
     ap.add_argument("--n", type=int, default=None, help="base size (profiling cases only)")
     ap.add_argument("--nq", type=int, default=None, help="queries per step (profiling cases only)")
     ap.add_argument("--tables", type=int, default=None, help="LSH tables (cross-polytope configurations)")
+    ap.add_argument("--fp64-recheck", type=int, default=-1, choices=[-1, 0, 1],
+                    help="lshg_options.fp64_recheck of the index (-1: the library default)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.config:
@@ -407,6 +414,7 @@ def main():
         globals()["N_QUERY"] = args.nq
     if args.tables is not None:
         globals()["CP_TABLES"] = args.tables
+    globals()["FP64_RECHECK"] = args.fp64_recheck
     args.path = args.path or "tc"
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -648,7 +656,8 @@ def main():
               or {"simhash": "u32", "wmh1": "u32"}.get(args.path, "f32")),
         "data": "synthetic",
         "config": {"workload": workload_text(args), "global_batch": N_QUERY * world,
-                   "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)"},
+                   "path": args.path, "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (no flush)",
+                   "fp64_recheck": FP64_RECHECK},
         "roofline": roofline,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": N_QUERY * (DIM + PAD_DIM) * 4,
                 "d2h_bytes_per_step": N_QUERY * K * 8, "api": e2e_api,

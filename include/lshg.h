@@ -83,11 +83,10 @@ typedef struct lshg_options_s {
   int cp_rounds;         /* cross-polytope rotation rounds (reference: 3, crossPolyTope.cuh:44) */
   void* stream;          /* cudaStream_t to run on, NULL = a library-owned stream */
   int fp64_recheck;      /* re-score, in double precision on the GPU, the re-ranked candidates
-                            whose FP32 distance lies within the FP32 error bound of a
-                            neighbour's (at the k-th place or anywhere among the first 256),
-                            and order those by the FP64 distance (ties: lower index); so the
-                            top-k is the FP64 top-k of the candidates for every k.  Returned
-                            distances stay FP32.  -1 (default) = on for the
+                            whose FP32 distance lies within the FP32 error bound of the k-th
+                            one (the run of near-ties around the k-th place), and order them
+                            by the FP64 distance (ties: lower index); so the top-k set is the
+                            FP64 top-k of the candidates.  Returned distances stay FP32.  -1 (default) = on for the
                             tensor-core scans (8, 9), off elsewhere; 0 = off; 1 = on for every
                             re-ranked scan (3-6, 8, 9).  The exact scan (2) returns the
                             reference's FP32 order. */

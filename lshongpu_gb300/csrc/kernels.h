@@ -86,9 +86,9 @@ int scan_bits_splits(int64_t n, int nq, int C);
 // Merge per-split sorted lists into one sorted list of C keys per query.
 void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
 // Exact re-rank of candidate keys (candidateSetScanner.cuh:10-32) and top-k output;
-// fp64_recheck: re-score, in double precision, the candidates whose FP32 distance lies
-// within the FP32 error bound of a neighbour's in the sorted list (among the first 256)
-// and order each such run by the FP64 distance.
+// fp64_recheck: re-score, in double precision, the run of candidates around the k-th
+// place whose FP32 distances lie within the FP32 error bound of one another (among the
+// first 128) and order that run by the FP64 distance.
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d,
                    const float* xnorm, const float* q, const float* qnorm, int dist, int k,
                    struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr, bool fp64_recheck = false,

@@ -8,11 +8,10 @@
 // 84-99).  Empty candidates (no point) become (-1, INT_MAX) as in the reference.
 //
 // FP64 re-check (optional, on by default for the tensor-core scans): after the FP32 sort,
-// the candidates whose FP32 distances lie within the FP32 error bound of a neighbour's --
-// the only ones whose order FP32 may get wrong, at the k-th place or anywhere else -- are
-// re-scored in double precision and reordered by (FP64 distance, id), so the top-k set and
-// its order are those of the exact distances for every k.  Returned distances stay the
-// FP32 values of the reference's formula.
+// the candidates whose FP32 distance lies within the FP32 error bound of the k-th one --
+// the only ones that FP32 may put on the wrong side of the k-th place -- are re-scored in
+// double precision and reordered by (FP64 distance, id), so the top-k set is that of the
+// exact distances.  Returned distances stay the FP32 values of the reference's formula.
 #include "common.cuh"
 #include "kernels.h"
 #include "launch_count.h"
@@ -25,25 +24,27 @@ namespace lshg {
 
 namespace {
 
-constexpr int kBandMax = 256;  // entries a query's FP64 band re-scores at most
+constexpr int kBandMax = 128;  // entries a query's FP64 re-check covers at most
 
-// Double-precision distance of float rows, same definition as the FP32 formula, computed
-// by a whole warp: lane l sums the terms of dimensions l, l + 32, ... in order (products of
-// floats are exact in double), then the 32 partial sums are added in a fixed tree to lane 0
-// and broadcast.  The GPU's FP64 pipe is narrow, and a warp instruction costs the same with
-// one active lane as with 32, so one lane walking a whole row would cost 32 times as much.
-// qq: the query's squared norm in double (angular only).
+// Double-precision closeness of a float row to the query as a ratio a / b (larger =
+// closer, b > 0), computed by a whole warp: lane l sums the terms of dimensions l, l + 32,
+// ... in order (products of floats are exact in double), then the 32 partial sums are added
+// in a fixed tree to lane 0 and broadcast.  The GPU's FP64 pipe is narrow, and a warp
+// instruction costs the same with one active lane as with 32, so one lane walking a whole
+// row would cost 32 times as much.
+//   angular   a = q.x, b = |x|      (1 - a / (|q| b) orders as -a / b; |q| is common)
+//   Jaccard   a = sum min, b = sum max
+//   Euclidean a = -sum (q - x)^2, b = 1
+// Two candidates are then ordered by comparing a_i b_j with a_j b_i in double: no division
+// or square root per candidate.  xn: the row's norm in double when the index keeps them.
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
   return __shfl_sync(0xffffffffu, v, 0);
 }
 
-// xn: the row's norm in double when the index keeps them (else computed here); qn: the
-// query's norm in double.
 template <int DIST>
-__device__ double fp64_distance_warp(const float* __restrict__ xr, const float* qr, int d, double qn, double xn,
-                                     int lane) {
+__device__ double2 fp64_closeness_warp(const float* __restrict__ xr, const float* qr, int d, double xn, int lane) {
   if (DIST == DIST_ANGULAR) {
     double dot = 0.0, xx = 0.0;
     if (xn > 0.0) {
@@ -56,8 +57,7 @@ __device__ double fp64_distance_warp(const float* __restrict__ xr, const float* 
       }
       xn = __dsqrt_rn(warp_sum_d(xx));
     }
-    dot = warp_sum_d(dot);
-    return __dadd_rn(1.0, -__ddiv_rn(dot, __dmul_rn(qn, xn)));
+    return make_double2(warp_sum_d(dot), xn);
   } else if (DIST == DIST_JACCARD) {
     double mn = 0.0, mx = 0.0;
     for (int j = lane; j < d; j += 32) {
@@ -65,98 +65,71 @@ __device__ double fp64_distance_warp(const float* __restrict__ xr, const float* 
       mn = __dadd_rn(mn, fmin(a, b));
       mx = __dadd_rn(mx, fmax(a, b));
     }
-    mn = warp_sum_d(mn);
-    mx = warp_sum_d(mx);
-    return __dadd_rn(1.0, -__ddiv_rn(mn, mx));
+    return make_double2(warp_sum_d(mn), warp_sum_d(mx));
   } else {
     double acc = 0.0;
     for (int j = lane; j < d; j += 32) {
       const double df = __dadd_rn((double)qr[j], -(double)xr[j]);
       acc = __dadd_rn(acc, __dmul_rn(df, df));
     }
-    acc = warp_sum_d(acc);
-    return DIST == DIST_EUCLID ? __dsqrt_rn(acc) : acc;
+    return make_double2(-warp_sum_d(acc), 1.0);
   }
 }
 
-__device__ __forceinline__ uint64_t double_to_ordered(double v) {
-  const uint64_t u = (uint64_t)__double_as_longlong(v == 0.0 ? 0.0 : v);
-  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-
-// Orders every run of near-tied candidates by FP64 distance.  After the FP32 sort, entry i
-// joins the run of entry i - 1 when their FP32 distances differ by at most the band (twice
-// the FP32 error bound, band_abs + band_rel * |distance|); two entries of different runs
-// are then in exact order, and each run of two or more entries is re-scored in double
-// precision and sorted by (FP64 distance, id).  The list is thus in FP64 order throughout,
-// so every prefix -- the top-k for any k -- is the FP64 top-k of the candidates.  Runs are
-// searched among the first kBandMax entries.  Called by every thread of the block after
-// the sort; qr is the query row.
+// FP64 re-check at the k-th place.  After the FP32 sort, the run of entries around entry
+// k - 1 whose consecutive FP32 distances differ by at most the band (twice the FP32 error
+// bound, band_abs + band_rel * |distance|) holds every candidate whose order against the
+// k-th could differ in exact arithmetic: outside it the FP32 order is the exact order.  A
+// run of two or more entries is re-scored in double precision and sorted by (FP64
+// closeness, id), so the top-k set -- and its order around the k-th place -- is that of
+// the exact distances.  The run is searched among the first kBandMax entries.  Called by
+// every thread of the block after the sort; qr is the query row.
 template <int DIST>
-__device__ void fp64_runs(uint64_t* keys, int C, int k, const float* __restrict__ x, const double* __restrict__ xn64,
-                          int d, const float* qr, float band_abs, float band_rel) {
+__device__ void fp64_boundary(uint64_t* keys, int C, int k, const float* __restrict__ x,
+                              const double* __restrict__ xn64, int d, const float* qr, float band_abs,
+                              float band_rel) {
+  __shared__ double2 s_ab[kBandMax];  // closeness a / b in double
   __shared__ uint64_t s_key[kBandMax];
-  __shared__ uint64_t s_ord[kBandMax];
-  __shared__ short s_run[kBandMax];   // first entry of the entry's run
-  __shared__ short s_len[kBandMax];   // length of the entry's run
-  __shared__ short s_list[kBandMax];  // entries in runs of two or more
-  __shared__ int s_nlist;
-  __shared__ double s_qn;
+  __shared__ int s_lo, s_hi;
   const int L = imin(C, kBandMax);
+  const int kk = imin(k, L) - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int i = threadIdx.x; i < L; i += blockDim.x) s_key[i] = keys[i];
-  __syncthreads();
+  if (kk < 0) return;
   if (threadIdx.x == 0) {
-    // runs up to the one holding entry k - 1: only the first k entries are returned, and
-    // the runs before it decide them
-    int start = 0, nl = 0;
-    for (int i = 1; i <= L; ++i) {
-      bool join = false;
-      if (i < L && s_key[i] != kEmptyKey && s_key[i - 1] != kEmptyKey) {
-        const float a = key_dist(s_key[i - 1]), b = key_dist(s_key[i]);
-        join = fabsf(b - a) <= band_abs + band_rel * fmaxf(fabsf(a), fabsf(b));
-      }
-      if (!join) {
-        for (int j = start; j < i; ++j) {
-          s_run[j] = (short)start;
-          s_len[j] = (short)(i - start);
-          if (i - start > 1) s_list[nl++] = (short)j;
-        }
-        start = i;
-        if (i >= k) break;
-      }
-    }
-    s_nlist = nl;
+    auto joined = [&](int i) {  // entries i - 1 and i are within the band
+      const uint64_t a = keys[i - 1], b = keys[i];
+      if (a == kEmptyKey || b == kEmptyKey) return false;
+      const float da = key_dist(a), db = key_dist(b);
+      return fabsf(db - da) <= band_abs + band_rel * fmaxf(fabsf(da), fabsf(db));
+    };
+    int lo = kk, hi = kk;
+    while (lo > 0 && joined(lo)) --lo;
+    while (hi + 1 < L && joined(hi + 1)) ++hi;
+    s_lo = lo;
+    s_hi = hi;
   }
   __syncthreads();
-  const int nl = s_nlist;
-  if (nl == 0) return;  // block-uniform
-  if (DIST == DIST_ANGULAR && warp == 0) {
-    double qq = 0.0;
-    for (int j = lane; j < d; j += 32) qq = __dadd_rn(qq, __dmul_rn((double)qr[j], (double)qr[j]));
-    qq = warp_sum_d(qq);
-    if (lane == 0) s_qn = __dsqrt_rn(qq);
+  const int lo = s_lo, m = s_hi - s_lo + 1;
+  if (m < 2) return;  // block-uniform
+  for (int t = threadIdx.x; t < m; t += blockDim.x) s_key[t] = keys[lo + t];
+  __syncthreads();
+  for (int t = warp; t < m; t += nwarps) {  // a warp a candidate
+    const int id = key_id(s_key[t]);
+    const double2 ab = fp64_closeness_warp<DIST>(x + (int64_t)id * d, qr, d, xn64 ? xn64[id] : 0.0, lane);
+    if (lane == 0) s_ab[t] = ab;
   }
   __syncthreads();
-  for (int t = warp; t < nl; t += nwarps) {  // a warp a candidate
-    const int i = s_list[t];
-    const int id = key_id(s_key[i]);
-    const double v = fp64_distance_warp<DIST>(x + (int64_t)id * d, qr, d, s_qn, xn64 ? xn64[id] : 0.0, lane);
-    if (lane == 0) s_ord[i] = double_to_ordered(v);
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < nl; t += blockDim.x) {
-    const int i = s_list[t];
-    const int len = s_len[i], r0 = s_run[i];
-    const uint64_t oi = s_ord[i];
-    const uint32_t ii = (uint32_t)key_id(s_key[i]);
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const double2 pi = s_ab[t];
+    const uint32_t ii = (uint32_t)key_id(s_key[t]);
     int r = 0;
-    for (int j = r0; j < r0 + len; ++j) {
-      const uint64_t oj = s_ord[j];
+    for (int j = 0; j < m; ++j) {
+      const double2 pj = s_ab[j];
+      const double lj = __dmul_rn(pj.x, pi.y), li = __dmul_rn(pi.x, pj.y);  // j closer: a_j b_i > a_i b_j
       const uint32_t ij = (uint32_t)key_id(s_key[j]);
-      r += (oj < oi) || (oj == oi && (ij < ii || (ij == ii && j < i)));
+      r += (lj > li) || (lj == li && (ij < ii || (ij == ii && j < t)));
     }
-    keys[r0 + r] = s_key[i];
+    keys[lo + r] = s_key[t];
   }
   __syncthreads();
 }
@@ -207,7 +180,7 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -298,7 +271,7 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_runs<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
   for (int i = tid; i < k; i += CH) {
     const uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -310,6 +283,91 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
     const uint64_t t0 = tc::global_ns();
     while (!tc::mbar_try_sleep(bar_a, pending, 20000u))
       if (tc::global_ns() - t0 > tc::kWaitNs) break;
+  }
+}
+
+// Long candidate lists (C >= 1024) in two kernels: the gather kernel scores one chunk of
+// blockDim candidates of one query a CTA (rows staged by bulk copies as above) and writes
+// their keys; small CTAs with nothing but the gather keep several chunks in flight an SM,
+// where one CTA a query walking all its chunks in turn waited on each.  The select kernel
+// then sorts each query's keys, applies the FP64 re-check and writes the first k.
+template <int DIST>
+__global__ void rerank_gather_kernel(const uint64_t* __restrict__ cand, int C, const float* __restrict__ x, int64_t n,
+                                     int d, const float* __restrict__ xnorm, const float* __restrict__ q,
+                                     const float* __restrict__ qnorm, uint64_t* __restrict__ keys_out, int* err) {
+  extern __shared__ __align__(128) unsigned char rsm[];
+  const int CH = blockDim.x;
+  const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
+  float* qr = reinterpret_cast<float*>(rsm + (size_t)CH * slot);
+  __shared__ __align__(8) uint64_t bar;
+  const int qi = blockIdx.y, tid = threadIdx.x, i = blockIdx.x * CH + tid;
+  const uint32_t bar_a = tc::smem_u32(&bar);
+  if (tid == 0) tc::mbar_init(bar_a, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
+  int id = -1;
+  if (i < C) {
+    const uint64_t kin = cand[(int64_t)qi * C + i];
+    if (kin != kEmptyKey) {
+      id = key_id(kin);
+      if (id < 0 || id >= n) id = -1;
+    }
+  }
+  const float qn = (DIST == DIST_ANGULAR) ? qnorm[qi] : 1.0f;
+  const float xn = (DIST == DIST_ANGULAR && id >= 0) ? xnorm[id] : 1.0f;
+  unsigned char* dst = rsm + (size_t)tid * slot;
+  const int nv = __syncthreads_count(id >= 0);
+  bool ok = false;
+  if (nv > 0) {
+    if (tid == 0) tc::mbar_expect_tx(bar_a, (uint32_t)nv * rowb);
+    __syncthreads();
+    if (id >= 0) tc::bulk_load(tc::smem_u32(dst), x + (int64_t)id * d, rowb, bar_a);
+    bool got = tc::mbar_try(bar_a, 0);
+    if (!got) {
+      const uint64_t t0 = tc::global_ns();
+      while (!(got = tc::mbar_try_sleep(bar_a, 0, 20000u)))
+        if (tc::global_ns() - t0 > tc::kWaitNs) break;
+    }
+    ok = __syncthreads_and(got);
+    if (!ok && tid == 0 && err) atomicExch(err, 3);
+  }
+  if (i < C) {
+    uint64_t ko = kEmptyKey;
+    if (id >= 0) {
+      const float dist =
+          ok ? exact_distance_v4<DIST, true>(reinterpret_cast<const float4*>(dst), reinterpret_cast<const float4*>(qr),
+                                             d >> 2, qn, xn)
+             : exact_distance<DIST>(x + (int64_t)id * d, qr, d, qn, xn);
+      ko = make_key(dist, id);
+    }
+    keys_out[(int64_t)qi * C + i] = ko;
+  }
+  if (nv > 0 && !ok) {  // a timed-out copy may still land: wait for it (bounded) before the block exits
+    const uint64_t t0 = tc::global_ns();
+    while (!tc::mbar_try_sleep(bar_a, 0, 20000u))
+      if (tc::global_ns() - t0 > tc::kWaitNs) break;
+  }
+}
+
+template <int DIST>
+__global__ void rerank_select_kernel(const uint64_t* __restrict__ keys_in, int C, const float* __restrict__ x, int d,
+                                     const float* __restrict__ q, int k, lshg_point* __restrict__ out, float band_abs,
+                                     float band_rel, const double* __restrict__ xn64) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(rsm);
+  float* qr = reinterpret_cast<float*>(rsm + (size_t)C * 8);
+  const int qi = blockIdx.x;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) qr[j] = q[(int64_t)qi * d + j];
+  for (int i = threadIdx.x; i < C; i += blockDim.x) keys[i] = keys_in[(int64_t)qi * C + i];
+  __syncthreads();
+  block_bitonic_sort(keys, C);
+  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    const uint64_t kk = i < C ? keys[i] : kEmptyKey;
+    lshg_point pt;
+    if (kk == kEmptyKey) { pt.ID = -1; pt.distance = kEmptyDistance; }
+    else { pt.ID = key_id(kk); pt.distance = key_dist(kk); }
+    out[(int64_t)qi * k + i] = pt;
   }
 }
 
@@ -369,7 +427,36 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
   // staged: rows of d % 4 == 0 floats, 16-byte aligned, up to 128 a chunk
   const int CH = std::min(C, 128);
   const size_t staged_smem = (size_t)CH * stage_slot_bytes(d) + (size_t)C * 8 + (size_t)d * 4 + 16;
-  if (d % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 && staged_smem <= 96 * 1024) {
+  const bool stageable = d % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+  const size_t gather_smem = (size_t)128 * stage_slot_bytes(d) + (size_t)d * 4 + 16;
+  const size_t select_smem = (size_t)C * 8 + (size_t)d * 4 + 16;
+  if (stageable && C >= 1024 && !test_stall && gather_smem <= 96 * 1024 && select_smem <= 200 * 1024) {
+    DevBuf<uint64_t> gk((size_t)nq * C, s);
+#define LSHG_RR2(DV)                                                                                            \
+  do {                                                                                                          \
+    LSHG_CUDA(cudaFuncSetAttribute(rerank_gather_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                   (int)gather_smem));                                                          \
+    rerank_gather_kernel<DV><<<dim3(C / 128, nq), 128, gather_smem, s>>>(cand, C, x, n, d, xnorm, q, qnorm,     \
+                                                                         gk.ptr, err);                          \
+    count_launch();                                                                                             \
+    LSHG_CHECK_LAUNCH();                                                                                        \
+    LSHG_CUDA(cudaFuncSetAttribute(rerank_select_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                   (int)select_smem));                                                          \
+    rerank_select_kernel<DV><<<nq, 512, select_smem, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel, xn64); \
+  } while (0)
+    switch (dist) {
+      case DIST_ANGULAR: LSHG_RR2(DIST_ANGULAR); break;
+      case DIST_JACCARD: LSHG_RR2(DIST_JACCARD); break;
+      case DIST_EUCLID: LSHG_RR2(DIST_EUCLID); break;
+      case DIST_SQEUCLID: LSHG_RR2(DIST_SQEUCLID); break;
+      default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "re-rank: invalid distance function");
+    }
+#undef LSHG_RR2
+    count_launch();
+    LSHG_CHECK_LAUNCH();
+    return;
+  }
+  if (stageable && staged_smem <= 96 * 1024) {
 #define LSHG_RRS(DV)                                                                                           \
   do {                                                                                                         \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_staged_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \

@@ -12,8 +12,9 @@
 //    so that requests arriving meanwhile join it.  Requests with different k share a
 //    launch when the index computes the same candidates for them (batch_class): the
 //    launch runs at the largest k and each request receives the first k of its rows,
-//    which is its own top-k (the lists are sorted, ties by lower index, and with the FP64
-//    re-check every near-tie run is in FP64 order).  The batch is padded to a power-of-two
+//    which is its own top-k (the lists are sorted, ties by lower index; an index with the
+//    FP64 re-check, which orders the near-ties around the k-th place, shares a launch only
+//    between requests of equal k).  The batch is padded to a power-of-two
 //    class by repeating its last query, copied into the slot's pinned buffer and launched;
 //    requests that arrive while other batches are on the GPU go to the next free slot, so
 //    their work overlaps on the device;
@@ -64,8 +65,12 @@ struct Request {
 // buckets do not depend on k.
 int batch_class(const Index& I, int k) {
   const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
+  // tensor-core scans with the FP64 re-check order the near-ties around the k-th place,
+  // which depends on k: only requests with the same k share a launch
+  if (I.p.framework == 0 && (impl == 8 || impl == 9) && I.p.opt.fp64_recheck != 0) return 1 << 20 | k;
   if (I.p.framework == 0 && impl == 8) return k <= 32 ? 0 : 1;
   if (I.p.framework == 0 && impl == 9) return 0;  // 128 candidates at every k
+  if (I.p.framework == 0 && I.p.opt.fp64_recheck > 0) return 1 << 20 | k;
   int kp = 32;
   while (kp < k) kp <<= 1;
   const bool sketched = I.p.framework == 0 ? (impl >= 3 && impl <= 6) : (I.p.runWithSketchedData && I.sk_kind);

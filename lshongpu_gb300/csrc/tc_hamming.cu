@@ -555,7 +555,7 @@ HammingPlan plan_hamming(int64_t n, int C) {
     p.cap = NT * HN;
     return p;
   }
-  for (int S : {8, 4, 2, 1}) {
+  for (int S : {16, 8, 4, 2, 1}) {
     const int NS = ceil_div(NT, S);
     const double m = (double)C / S;
     const int r = S == 1 ? C : std::min(C, (int)std::ceil(m + 4.0 * std::sqrt(m) + 8.0));
