@@ -166,7 +166,11 @@ void make_sketch(const Index& idx, const float* v, int64_t rows, uint8_t padbyte
   switch (idx.sk_kind) {
     case 3: {
       DevBuf<uint32_t> raw(rows * idx.words, s);
-      launch_project(v, rows, d, idx.sk_planes.ptr, idx.words * 32, 0, 32, idx.words, raw.ptr, nullptr, s);
+      if (idx.sk_split.ptr)  // tensor cores, bit-identical (exact recheck of the near-zero signs)
+        tc::launch_tc_signs(v, rows, d, idx.sk_split.ptr, idx.sk_pnorm.ptr, idx.sk_planes.ptr, idx.words * 32,
+                            idx.words, raw.ptr, err, s);
+      else
+        launch_project(v, rows, d, idx.sk_planes.ptr, idx.words * 32, 0, 32, idx.words, raw.ptr, nullptr, s);
       packed->alloc(rows * idx.wp, s);
       launch_pad_words(raw.ptr, rows, idx.words, packed->ptr, idx.wp, 0u, s);
       break;
@@ -273,11 +277,20 @@ int* Index::error_word(cudaStream_t s) {
   return w;
 }
 
+void derive_simhash(Index& I, cudaStream_t s) {
+  if (I.sk_kind != 3 || I.d > 128 || I.d < 1 || !I.sk_planes.ptr) return;
+  const int P = I.words * 32;
+  const int64_t ppad = (int64_t)(P + 255) / 256 * 256;
+  I.sk_split.alloc((size_t)ppad * 3 * tc::signs_part_cols(I.d), s);
+  I.sk_pnorm.alloc((size_t)ppad, s);
+  tc::launch_split_bf16(I.sk_planes.ptr, P, I.d, ppad, 1, I.sk_split.ptr, I.sk_pnorm.ptr, s);
+}
+
 Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
   for (auto& kv : err_words) cudaFree(kv.second);  // cudaFree waits for work that may still write it
   x.release(); xnorm.release(); xt.release(); xs.release(); xse.release(); xsf.release(); xsft.release();
-  sk_planes.release();
+  sk_planes.release(); sk_split.release(); sk_pnorm.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
   xbf.release(); xbf_scale.release(); xf8.release(); xnorm64.release(); xst.release(); qstats.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
@@ -412,6 +425,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
         std::vector<float> R((size_t)d * 32 * p.sketchDim);
         random_normals((int64_t)R.size(), 1.0, R.data());  // simHash.cu:73 / lshFramework.cuh:24-27
         upload(I.sk_planes, R.data(), R.size(), s);
+        derive_simhash(I, s);
         break;
       }
       case 4:

@@ -60,6 +60,9 @@ struct Index {
                              // [ceil(n/256)*256][128 * ceil(words/4)] (derived, not stored)
   DevBuf<float> xsf, xsft;   // JL sketches [n][sdim] and their tile layout
   DevBuf<float> sk_planes;   // SimHash planes [32*sketchDim][d] or JL rows [sdim][d]
+  DevBuf<uint16_t> sk_split; // SimHash planes split into BF16 [hi | lo | hi] rows for the
+                             // tensor-core projection (d <= 128; derived, not stored)
+  DevBuf<float> sk_pnorm;    // their norms, rows padded to 256
   WmhState wmh_sk;
 
   // LSH
@@ -125,8 +128,10 @@ int next_pow2(int v);
 // Jaccard sketches of at most 1024 bits idx.xse (their E4M3 rows for the tensor cores).
 void tile_sketches(Index& idx, cudaStream_t stream);
 
-// Arrays derived from stored ones at build and at load: the tensor-core scans' FP64 row norms.
+// Arrays derived from stored ones at build and at load: the tensor-core scans' FP64 row norms,
+// and the split SimHash planes of the tensor-core projection.
 void derive_tc(Index& idx, cudaStream_t stream);
+void derive_simhash(Index& idx, cudaStream_t stream);
 
 // Persistence (persist.cpp): checksummed binary image of a built index.
 void save_index(const Index& idx, const char* path);

@@ -42,6 +42,10 @@ void launch_pad_words(const uint32_t* in, int64_t n, int words, uint32_t* out, i
 // mode 1: floats (JL, simHashJL.cuh:34-51): out_f[i*planes + p].
 void launch_project(const float* x, int64_t n, int d, const float* planes, int nplanes, int mode,
                     int bits, int words, uint32_t* out32, float* out_f, cudaStream_t s);
+// Sign bits of 32-plane words as above, run only when *gate != 0 (read on the device: the
+// blocks leave at once otherwise).
+void launch_project_gated(const float* x, int64_t n, int d, const float* planes, int nplanes, int words,
+                          uint32_t* out32, const int* gate, cudaStream_t s);
 
 // ---- crosspoly.cu ----------------------------------------------------------------
 // Cross-polytope keys (crossPolyTope.cuh:25-85) with `hashes` concatenated hashes per

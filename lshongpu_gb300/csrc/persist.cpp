@@ -405,6 +405,7 @@ std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
   for (auto& kv : r.staged) kv.second.upload(s);
   if (I.p.framework == 0 && I.xs.n) tile_sketches(I, s);  // derived layouts, not stored
   if (I.p.framework == 0 && (I.p.implementation == 8 || I.p.implementation == 9)) derive_tc(I, s);
+  derive_simhash(I, s);
   I.qstats.alloc(2, s);
   LSHG_CUDA(cudaMemsetAsync(I.qstats.ptr, 0, I.qstats.bytes(), s));
   LSHG_CUDA(cudaStreamSynchronize(s));

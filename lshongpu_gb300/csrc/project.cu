@@ -22,7 +22,9 @@ constexpr int kPitch = 68;   // shared row pitch (floats), keeps float4 alignmen
 __global__ void __launch_bounds__(256) project_kernel(const float* __restrict__ x, int64_t n, int d,
                                                       const float* __restrict__ planes, int nplanes,
                                                       int mode, int bits, int words,
-                                                      uint32_t* __restrict__ out32, float* __restrict__ outf) {
+                                                      uint32_t* __restrict__ out32, float* __restrict__ outf,
+                                                      const int* __restrict__ gate) {
+  if (gate && *gate == 0) return;  // block-uniform
   extern __shared__ __align__(16) float sm[];
   float* xs = sm;                 // [d][kPitch]
   float* rs = sm + d * kPitch;    // [d][kPitch]
@@ -116,7 +118,19 @@ void launch_project(const float* x, int64_t n, int d, const float* planes, int n
   ProfScope _ps(mode == 1 ? "project_jl" : "project_simhash", s);
   LSHG_CUDA(cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(ceil_div(n, kTP), ceil_div(nplanes, kTL));
-  project_kernel<<<grid, 256, smem, s>>>(x, n, d, planes, nplanes, mode, bits, words, out32, out_f);
+  project_kernel<<<grid, 256, smem, s>>>(x, n, d, planes, nplanes, mode, bits, words, out32, out_f, nullptr);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_project_gated(const float* x, int64_t n, int d, const float* planes, int nplanes, int words,
+                          uint32_t* out32, const int* gate, cudaStream_t s) {
+  if (n <= 0 || nplanes <= 0) return;
+  size_t smem = (size_t)2 * d * kPitch * sizeof(float);
+  LSHG_REQUIRE(smem <= 220 * 1024 && nplanes == 32 * words, "bad projection shape");
+  LSHG_CUDA(cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(ceil_div(n, kTP), ceil_div(nplanes, kTL));
+  project_kernel<<<grid, 256, smem, s>>>(x, n, d, planes, nplanes, 0, 32, words, out32, nullptr, gate);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }

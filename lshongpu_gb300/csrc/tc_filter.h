@@ -74,6 +74,16 @@ void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int w
 // Rows of kp bytes (a multiple of 16); boxes of 128 bytes x box_rows rows, 128-byte swizzle.
 CUtensorMap make_map_bytes(const void* base, int64_t rows, int kp, int box_rows);
 
+// SimHash sign bits on the tensor cores (tc_hamming.cu), bit-identical to project_kernel:
+// a split-BF16 GEMM decides every sign outside a band around zero, the signs inside it are
+// recomputed with the reference's FMA chain.  planes_split / pnorm: launch_split_bf16 of
+// the planes (order 1, rows padded to 256) and their norms; out32 [n][words].
+int signs_part_cols(int d);
+void launch_split_bf16(const float* x, int64_t n, int d, int64_t rows_pad, int order, uint16_t* out, float* norms,
+                       cudaStream_t s);
+void launch_tc_signs(const float* x, int64_t n, int d, const uint16_t* planes_split, const float* pnorm,
+                     const float* planes, int P, int words, uint32_t* out32, int* err, cudaStream_t s);
+
 void launch_gather_rows(const uint16_t* src, const int* ovf, int nq, uint16_t* dst, cudaStream_t s);
 
 void launch_merge_fallback(const uint64_t* part, const int* ovf, int nq, int NT, int grid, int CT, uint64_t* out,

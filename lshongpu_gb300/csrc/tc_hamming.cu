@@ -49,6 +49,8 @@
 #include "tc_filter.h"
 #include "tc_ptx.cuh"
 
+#include <cuda_bf16.h>
+
 namespace lshg {
 
 int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, const uint32_t* qs, int nq, int op,
@@ -85,8 +87,10 @@ struct HLayout {
   static constexpr int BAR_OFF = S_OFF + 4 * SBUF * BM * 8;
   static constexpr int SMEM = BAR_OFF + 256 + 1024;
   static_assert(SMEM <= kSmemLimit, "shared memory per CTA");
-  static_assert(8 * (2 * STAGES + 2 + 2 * H_NACC + 1) + 8 <= 256, "barrier area");
+  static_assert(8 * (2 * STAGES + 2 + 2 * H_NACC + 1) + 12 <= 256, "barrier area");
 };
+
+constexpr int MODE_SIGNS = 2;  // SimHash projections: sign bits, uncertain ones listed
 
 struct HArgs {
   int nq;
@@ -103,6 +107,15 @@ struct HArgs {
   uint64_t* cand;   // [nq][cap] survivor keys
   int cap;
   int* err;
+  // MODE_SIGNS: rows are points, the "base" is the planes
+  const float* rown;   // point norms
+  const float* pnorm;  // plane norms (padded to whole tiles with zeros)
+  float band;          // a sign is certain when |score| > band * |x| * |r|
+  uint32_t* out32;     // [nq][words] sign bits
+  int words, P;        // words a point, planes (32 * words)
+  uint2* list;         // [grid][list_cap] (point, plane) of the uncertain signs, a segment a CTA
+  int* list_cnt;       // [grid] entries a segment (may exceed list_cap: overflow)
+  int list_cap;
 };
 
 // Out of line: called from every group of the unrolled survivor path, inlined copies would
@@ -113,13 +126,14 @@ __device__ __noinline__ void h_flush(int* cnt, uint64_t* dst, int cap, const flo
     if (base + e < cap) dst[base + e] = make_key(-ssc[e * BM], sid[e * BM]);
 }
 
-template <int MODE, int GW, int KC>
+// BF: operands are BF16 (kind::f16, 64 elements a 128-byte chunk) instead of E4M3.
+template <int MODE, int GW, int KC, bool BF = false>
 __global__ void __launch_bounds__(H_THREADS, 1)
     tc_hamming_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                       const HArgs a) {
   using LY = HLayout<KC>;
   constexpr int STAGES = LY::STAGES, SBUF = LY::SBUF;
-  static_assert(MODE == MODE_GROUPMAX || GW == 64, "the filter reads whole 64-column pieces");
+  static_assert(MODE != MODE_FILTER || GW == 64, "the filter reads whole 64-column pieces");
   static_assert(GW == 64 || GW == 8, "group width");
   const int U = a.NCH * a.QT;
   if ((int)blockIdx.x >= U) return;  // no unit for this CTA: leave before any barrier or TMEM use
@@ -154,6 +168,7 @@ __global__ void __launch_bounds__(H_THREADS, 1)
     }
     mbar_init(DONE, 1);
     *abort_flag = 0;
+    *reinterpret_cast<int*>(tmem_slot + 2) = 0;  // MODE_SIGNS list count
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 2) tmem_alloc(smem_u32(tmem_slot), H_TMEM_COLS);
@@ -201,7 +216,7 @@ __global__ void __launch_bounds__(H_THREADS, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_e4m3(BM, HN);
+      constexpr uint32_t idesc = BF ? idesc_bf16(BM, HN) : idesc_e4m3(BM, HN);
       int it = 0, ia = 0, ua = 0;
       bool ok = true;
       for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
@@ -221,9 +236,14 @@ __global__ void __launch_bounds__(H_THREADS, 1)
             const uint32_t a_base = s0 + LY::A_OFF + kc * BM * H_CHUNK;
             const uint32_t b_base = s0 + LY::B_OFF + st * LY::B_BYTES;
 #pragma unroll
-            for (int kk = 0; kk < H_CHUNK / 32; ++kk)
-              umma_e4m3(d_tmem, smem_desc(a_base + kk * 32), smem_desc(b_base + kk * 32), idesc,
-                        (kc > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < H_CHUNK / 32; ++kk) {  // 32 bytes a step: K = 32 E4M3 or 16 BF16
+              if (BF)
+                umma_bf16(d_tmem, smem_desc(a_base + kk * 32), smem_desc(b_base + kk * 32), idesc,
+                          (kc > 0 || kk > 0) ? 1u : 0u);
+              else
+                umma_e4m3(d_tmem, smem_desc(a_base + kk * 32), smem_desc(b_base + kk * 32), idesc,
+                          (kc > 0 || kk > 0) ? 1u : 0u);
+            }
             umma_commit(EMPTY(st));
             ++it;
           }
@@ -248,6 +268,8 @@ __global__ void __launch_bounds__(H_THREADS, 1)
     int scnt = 0;
     int ia = 0;
     bool ok = true;
+    int* seg_cnt = reinterpret_cast<int*>(tmem_slot + 2);  // MODE_SIGNS: this CTA's list count
+    uint2* seg = MODE == MODE_SIGNS ? a.list + (int64_t)blockIdx.x * a.list_cap : nullptr;
     for (int u = blockIdx.x; u < U && ok; u += gridDim.x) {
       const int qt = u % a.QT, c = u / a.QT;
       const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
@@ -267,7 +289,35 @@ __global__ void __launch_bounds__(H_THREADS, 1)
         ++ia;
         const int64_t cbase = (int64_t)p * a.dstride * HN + g * 64;  // base id of v[0]
         const int piece = 4 * p + g;
-        if (MODE == MODE_GROUPMAX) {
+        if (MODE == MODE_SIGNS) {
+          // bit = score >= 0, as the reference's sign test; a sign within the split-BF16
+          // error bound of zero is listed for the exact recheck
+          if (q < a.nq && cbase < a.P) {
+            const float bx = a.band * a.rown[q];
+            const float4* pn4 = reinterpret_cast<const float4*>(a.pnorm + cbase);
+            uint32_t w0 = 0, w1 = 0;
+#pragma unroll
+            for (int j4 = 0; j4 < 16; ++j4) {
+              const float4 pn = __ldg(pn4 + j4);
+              const float pv[4] = {pn.x, pn.y, pn.z, pn.w};
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const int j = 4 * j4 + e;
+                const float sc = __uint_as_float(v[j]);
+                const uint32_t bit = sc >= 0.0f ? 1u : 0u;
+                if (j < 32) w0 |= bit << j;
+                else w1 |= bit << (j - 32);
+                if (fabsf(sc) <= bx * pv[e] && cbase + j < a.P) {
+                  const int pos = atomicAdd(seg_cnt, 1);
+                  if (pos < a.list_cap) seg[pos] = make_uint2((uint32_t)q, (uint32_t)(cbase + j));
+                }
+              }
+            }
+            uint32_t* row = a.out32 + (int64_t)q * a.words + (cbase >> 5);
+            row[0] = w0;
+            if (cbase + 32 < a.P) row[1] = w1;
+          }
+        } else if (MODE == MODE_GROUPMAX) {
           if (cbase + 64 > a.n) {  // last base tile: padding rows are not points
 #pragma unroll
             for (int j = 0; j < 64; ++j)
@@ -347,6 +397,7 @@ __global__ void __launch_bounds__(H_THREADS, 1)
     tmem_dealloc(tmem, H_TMEM_COLS);
   }
   if (threadIdx.x == 0 && *abort_flag) atomicExch(a.err, 2);
+  if (MODE == MODE_SIGNS && threadIdx.x == 0) a.list_cnt[blockIdx.x] = *reinterpret_cast<int*>(tmem_slot + 2);
 }
 
 // Sketch rows of wp words (the first `words` real) -> E4M3 rows of kp bytes: bit b of word w
@@ -506,15 +557,17 @@ CUtensorMap map_sketch_rows(const void* base, int64_t rows, int kp, int box_rows
   return make_map_bytes(base, rows, kp, box_rows);
 }
 
-template <int MODE, int GW, int KC>
-void run_hamming(const CUtensorMap& ma, const CUtensorMap& mb, HArgs a, const char* name, cudaStream_t s) {
+template <int MODE, int GW, int KC, bool BF = false>
+void run_hamming(const CUtensorMap& ma, const CUtensorMap& mb, HArgs a, const char* name, cudaStream_t s,
+                 int* grid_out = nullptr) {
   const int G = num_sms();
   const int64_t work = (int64_t)a.NP * a.QT;
   a.CH = (int)std::max<int64_t>(1, std::min<int64_t>(32, (work + 8 * G - 1) / (8 * G)));
   a.NCH = ceil_div(a.NP, a.CH);
   const int U = a.NCH * a.QT;
   const int grid = std::min(G, U);
-  auto kern = tc_hamming_kernel<MODE, GW, KC>;
+  if (grid_out) *grid_out = grid;
+  auto kern = tc_hamming_kernel<MODE, GW, KC, BF>;
   constexpr int smem = HLayout<KC>::SMEM;
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   ProfScope _ps(name, s);
@@ -539,7 +592,127 @@ void run_hamming_kc(int kc, const CUtensorMap& ma, const CUtensorMap& mb, const 
   }
 }
 
+// ---- SimHash projections on the tensor cores ---------------------------------------------
+// A float v is split into two BF16 values hi = bf16(v), lo = bf16(v - hi) (the subtraction
+// is exact), so v - hi - lo is within 2^-16 |v|.  Points become rows [hi | hi | lo] and
+// planes [hi | lo | hi] (each part padded to kp columns), and one BF16 GEMM with K = 3 kp
+// gives x_hi r_hi + x_hi r_lo + x_lo r_hi, within 3 * 2^-16 sum |x_j r_j| <= 3 * 2^-16 |x||r|
+// of the exact x.r before the FP32 accumulation's own rounding.  norms: the rows' L2 norms.
+__global__ void split_bf16_kernel(const float* __restrict__ x, int64_t n, int d, int kp, int64_t rows_pad, int order,
+                                  __nv_bfloat16* __restrict__ out, float* __restrict__ norms) {
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < rows_pad; i += nw) {
+    __nv_bfloat16* row = out + i * 3 * kp;
+    float ss = 0.0f;
+    for (int j = lane; j < kp; j += 32) {
+      const float v = (i < n && j < d) ? x[i * d + j] : 0.0f;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+      row[j] = hi;
+      row[kp + j] = order == 0 ? hi : lo;
+      row[2 * kp + j] = order == 0 ? lo : hi;
+      ss = fmaf(v, v, ss);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    if (lane == 0) norms[i] = sqrtf(ss);
+  }
+}
+
+// Exact signs of the listed (point, plane) pairs: the reference's single-precision FMA chain
+// over the dimensions in order (the same arithmetic as project_kernel), written into the
+// sign bit.  A segment whose count exceeds its capacity raises *overflow.
+__global__ void sign_recheck_kernel(const uint2* __restrict__ list, const int* __restrict__ cnt, int cap, int segs,
+                                    const float* __restrict__ x, const float* __restrict__ planes, int d,
+                                    uint32_t* __restrict__ out32, int words, int* __restrict__ overflow) {
+  const int64_t total = (int64_t)segs * cap;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int seg = (int)(t / cap), i = (int)(t - (int64_t)seg * cap);
+    const int c = cnt[seg];
+    if (i == 0 && c > cap) atomicExch(overflow, 1);
+    if (i >= c) continue;
+    const uint2 e = list[t];
+    const float* xr = x + (int64_t)e.x * d;
+    const float* rr = planes + (int64_t)e.y * d;
+    float acc = 0.0f;
+    for (int j = 0; j < d; ++j) acc = __fmaf_rn(xr[j], rr[j], acc);
+    uint32_t* w = out32 + (int64_t)e.x * words + (e.y >> 5);
+    const uint32_t bit = 1u << (e.y & 31);
+    if (acc >= 0.0f) atomicOr(w, bit);
+    else atomicAnd(w, ~bit);
+  }
+}
+
 }  // namespace
+
+int signs_part_cols(int d) { return d <= 64 ? 64 : 128; }
+
+void launch_split_bf16(const float* x, int64_t n, int d, int64_t rows_pad, int order, uint16_t* out, float* norms,
+                       cudaStream_t s) {
+  LSHG_REQUIRE(d >= 1 && d <= 128, "tensor-core projections: d must be <= 128");
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((rows_pad * 32 + 255) / 256, (int64_t)num_sms() * 16));
+  split_bf16_kernel<<<blocks, 256, 0, s>>>(x, n, d, signs_part_cols(d), rows_pad, order,
+                                           reinterpret_cast<__nv_bfloat16*>(out), norms);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
+void launch_tc_signs(const float* x, int64_t n, int d, const uint16_t* planes_split, const float* pnorm,
+                     const float* planes, int P, int words, uint32_t* out32, int* err, cudaStream_t s) {
+  if (n <= 0) return;
+  LSHG_REQUIRE(P == 32 * words && P >= 32, "tensor-core projections: whole 32-plane words");
+  const int kp = signs_part_cols(d), kc = 3 * kp * 2 / H_CHUNK;
+  const int64_t rows_pad = (int64_t)ceil_div(n, BM) * BM;
+  const int64_t ppad = (int64_t)ceil_div(P, HN) * HN;
+  LSHG_REQUIRE(rows_pad / BM * (ppad / HN) < (int64_t)INT_MAX, "tensor-core projections: problem too large");
+  ProfScope _ps("tc_project", s);
+  DevBuf<uint16_t> xa((size_t)rows_pad * 3 * kp, s);
+  DevBuf<float> xn((size_t)rows_pad, s);
+  launch_split_bf16(x, n, d, rows_pad, 0, xa.ptr, xn.ptr, s);
+  const CUtensorMap ma = map_sketch_rows(xa.ptr, rows_pad, 6 * kp, BM);
+  const CUtensorMap mb = map_sketch_rows(planes_split, ppad, 6 * kp, HN);
+  // about 0.1% of the signs of unit points and N(0, 1) planes fall inside the band; each
+  // CTA's segment holds 4x its share, and the SIMT projection redoes everything if one
+  // overflows
+  const int G = num_sms();
+  const int64_t expect = (int64_t)n * P / 1000 / G + 1;
+  const int cap = (int)std::min<int64_t>(1 << 22, std::max<int64_t>(4096, 4 * expect));
+  DevBuf<uint2> list((size_t)G * cap, s);
+  DevBuf<int> cnt((size_t)G + 1, s);
+  LSHG_CUDA(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes(), s));
+  HArgs a{};
+  a.nq = (int)n;
+  a.n = P;
+  a.QT = (int)(rows_pad / BM);
+  a.NP = (int)(ppad / HN);
+  a.dstride = 1;
+  a.err = err;
+  a.rown = xn.ptr;
+  a.pnorm = pnorm;
+  a.band = 1.0f / 8192.0f;  // 2^-13: 2.7x the split's 3 * 2^-16, plus the accumulations' rounding
+  a.out32 = out32;
+  a.words = words;
+  a.P = P;
+  a.list = list.ptr;
+  a.list_cnt = cnt.ptr;
+  a.list_cap = cap;
+  int grid = 0;
+  if (kc == 3) run_hamming<MODE_SIGNS, 64, 3, true>(ma, mb, a, "tc_project_gemm", s, &grid);
+  else run_hamming<MODE_SIGNS, 64, 6, true>(ma, mb, a, "tc_project_gemm", s, &grid);
+  int* overflow = cnt.ptr + G;
+  {
+    const int64_t total = (int64_t)grid * cap;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)G * 16));
+    sign_recheck_kernel<<<blocks, 256, 0, s>>>(list.ptr, cnt.ptr, cap, grid, x, planes, d, out32, words, overflow);
+    count_launch();
+    LSHG_CHECK_LAUNCH();
+  }
+  // an overflowing segment lost entries: the SIMT projection then redoes every sign (its
+  // blocks leave at once when nothing overflowed)
+  launch_project_gated(x, n, d, planes, P, words, out32, overflow, s);
+}
 
 HammingPlan plan_hamming(int64_t n, int C) {
   HammingPlan p{};

@@ -103,6 +103,33 @@ def test_simhash_sketch_bits(engine, orc, words):
     assert np.array_equal(qs, orc.simhash(q, planes, words, 32))
 
 
+def test_simhash_tensor_core_projection_large(engine, orc):
+    """30,000 points x 1,024 planes: the tensor-core projection (split-BF16 GEMM, then the
+    reference's FMA chain for the signs inside the GEMM's error band) equals the oracle's
+    sign bits exactly, for the base (export) and for a query batch."""
+    words, n, nq = 32, 30000, 2000
+    x, q = data(n, nq, seed=91)
+    idx = engine.Index(x, implementation=3, sketchDim=words)
+    planes = engine.random_normals(D * 32 * words)
+    sk = np.frombuffer(idx.export(engine.EXPORT_SKETCHES), np.uint32).reshape(n, words)
+    assert np.array_equal(sk, orc.simhash(x, planes, words, 32))
+    qs, _ = idx.sketch_queries(q, np.uint32, words)
+    assert np.array_equal(qs, orc.simhash(q, planes, words, 32))
+
+
+def test_simhash_projection_band_overflow(engine, orc):
+    """Zero rows put every sign of theirs inside the band (0 >= 0 is a 1 bit): the recheck
+    lists overflow and the SIMT projection redoes the batch; bits still equal the oracle's."""
+    words, n = 8, 12000
+    x, _ = data(n, 1, seed=93)
+    x[::2] = 0.0
+    idx = engine.Index(x, implementation=3, sketchDim=words)
+    planes = engine.random_normals(D * 32 * words)
+    sk = np.frombuffer(idx.export(engine.EXPORT_SKETCHES), np.uint32).reshape(n, words)
+    assert np.array_equal(sk, orc.simhash(x, planes, words, 32))
+    assert np.all(sk[::2] == 0xFFFFFFFF)
+
+
 # C picks the scan's layout: 32, 8 or 2 queries a CTA with append buffers checked every
 # 1, 2 or 4 tiles; 32 words (1024 bits) runs the width-specialised kernel, 8 the generic one
 @pytest.mark.parametrize("C,n,words", [(128, 6000, 8), (256, 6000, 8), (1024, 6000, 8), (1024, 40000, 8),
