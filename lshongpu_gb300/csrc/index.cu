@@ -33,6 +33,13 @@ void tile_sketches(Index& I, cudaStream_t s) {
   const int64_t tiles = (I.n + 127) / 128;
   I.xst.alloc((size_t)tiles * 128 * I.wp, s);
   launch_tile_sketches(I.xs.ptr, I.n, I.wp, I.xst.ptr, s);
+  if (I.sk_kind == 4 && I.p.opt.sketch_scan != 1) {  // bit-sliced copy for the threshold-filter scan
+    const int wsl = byte_slice_words(I.wp);
+    DevBuf<uint32_t> sl((size_t)I.n * wsl, s);
+    launch_slice_bytes(I.xs.ptr, I.n, I.wp, I.n, 0x00, sl.ptr, s);
+    I.xsl.alloc((size_t)tiles * 128 * wsl, s);
+    launch_tile_sketches(sl.ptr, I.n, wsl, I.xsl.ptr, s);
+  }
   if ((I.sk_kind == 3 || I.sk_kind == 5) && I.words <= 32 && I.p.opt.sketch_scan != 1) {
     const int64_t rows = (I.n + 255) / 256 * 256;
     I.xse.alloc((size_t)rows * 128 * tc::hamming_chunks(I.words), s);
@@ -45,7 +52,8 @@ size_t wmh_state_bytes();
 size_t lsh_query_smem(const LshQueryArgs& a);
 int lsh_query_grid(int nq);
 void lsh_query_plan(LshQueryArgs& a, int max_grid);
-void launch_tc_scan(Index& idx, const float* q, int nq, int k, lshg_point* out, cudaStream_t s);
+void launch_tc_scan(Index& idx, const float* q, int nq, int k, lshg_point* out, cudaStream_t s,
+                    const RerankBounds* extra);
 void tc_prepare(Index& idx, cudaStream_t s);
 
 namespace {
@@ -289,7 +297,7 @@ void derive_simhash(Index& I, cudaStream_t s) {
 Index::~Index() {
   if (stream) cudaStreamSynchronize(stream);
   for (auto& kv : err_words) cudaFree(kv.second);  // cudaFree waits for work that may still write it
-  x.release(); xnorm.release(); xt.release(); xs.release(); xse.release(); xsf.release(); xsft.release();
+  x.release(); xnorm.release(); xt.release(); xs.release(); xse.release(); xsl.release(); xsf.release(); xsft.release();
   sk_planes.release(); sk_split.release(); sk_pnorm.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
   xbf.release(); xbf_scale.release(); xf8.release(); xnorm64.release(); xst.release(); qstats.release();
@@ -511,7 +519,7 @@ void query_error(Index& I, cudaStream_t s) {
   }
 }
 
-void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
+void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_t s, const RerankBounds* extra) {
   LSHG_REQUIRE(k >= 1 && k <= 4096, "k must be in [1, 4096]");
   if (nq <= 0) return;
   const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
@@ -566,7 +574,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     return;
   }
   if (impl == 8 || impl == 9) {
-    launch_tc_scan(I, q, nq, k, out, s);
+    launch_tc_scan(I, q, nq, k, out, s, extra);
     return;
   }
   if (impl == 2) {
@@ -599,7 +607,17 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
       part.alloc((size_t)nq * C, s);
       tc::launch_tc_hamming(I.xse.ptr, I.n, I.xst.ptr, I.wp, I.words, qs.ptr, nq, op, C, part.ptr, I.error_word(s), s);
       launch_rerank(part.ptr, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
-                    I.p.opt.fp64_recheck > 0);
+                    I.p.opt.fp64_recheck > 0, nullptr, extra);
+      return;
+    }
+    int fs = 0, fr = 0, fc = 0;
+    if (I.xsl.ptr && C > 128 && (mode == 2 || (mode == 0 && nq >= kTcSketchMinQueries)) &&
+        byte_filter_plan(I.n, C, &fs, &fr, &fc)) {
+      // byte samples: bit-sliced threshold filter, the exact top-C, then the same re-rank
+      part.alloc((size_t)nq * C, s);
+      launch_byte_filter_scan(I.xsl.ptr, I.xst.ptr, I.n, I.wp, I.sbytes, qs.ptr, nq, C, part.ptr, s);
+      launch_rerank(part.ptr, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
+                    I.p.opt.fp64_recheck > 0, nullptr, extra);
       return;
     }
     splits = scan_bits_splits(I.n, nq, C);
@@ -614,7 +632,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
     cand = merged.ptr;
   }
   launch_rerank(cand, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
-                I.p.opt.fp64_recheck > 0);
+                I.p.opt.fp64_recheck > 0, nullptr, extra);
 }
 
 }  // namespace lshg

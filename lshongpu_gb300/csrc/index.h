@@ -56,6 +56,8 @@ struct Index {
   int words = 0, wp = 0, sbytes = 0, sdim = 0;
   DevBuf<uint32_t> xs;       // packed sketches, rows of wp words
   DevBuf<uint32_t> xst;      // linear scans: the same, tiled [ceil(N/128)][wp/4][128] x 16 B
+  DevBuf<uint32_t> xsl;      // byte samples bit-sliced and tiled like xst, for the threshold-filter
+                             // scan (derived, not stored)
   DevBuf<uint8_t> xse;       // tensor-core sketch scans: sketch bits as E4M3 +-1 rows,
                              // [ceil(n/256)*256][128 * ceil(words/4)] (derived, not stored)
   DevBuf<float> xsf, xsft;   // JL sketches [n][sdim] and their tile layout
@@ -111,7 +113,10 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
 // query buffer is transformed in place.  Stream-ordered with no host synchronisation
 // and no pageable copies, so it can be recorded into a CUDA graph; callers check
 // query_error() after the stream has completed.
-void query_index(Index& idx, float* q, int nq, int k, lshg_point* out, cudaStream_t stream);
+// extra (optional, device memory): further places (< k) whose near-ties the FP64 re-check
+// orders, for callers that answer requests of smaller k from this launch's first rows.
+void query_index(Index& idx, float* q, int nq, int k, lshg_point* out, cudaStream_t stream,
+                 const RerankBounds* extra = nullptr);
 // Throws if a completed query on `stream` raised that stream's device error word (clears it).
 void query_error(Index& idx, cudaStream_t stream);
 // Throws LSHG_ERR_INVALID_ARGUMENT unless the calling thread's current device is the

@@ -86,9 +86,31 @@ int launch_scan_bits(const uint32_t* xst, int64_t n, int wp, int words, int sbyt
 void launch_tile_sketches(const uint32_t* xs, int64_t n, int wp, uint32_t* xst, cudaStream_t s);
 int scan_bits_splits(int64_t n, int nq, int C);
 
+// ---- scan_filter.cu ---------------------------------------------------------------
+// Byte weighted-MinHash samples bit-sliced: rows of byte_slice_words(wp) words (8 a group
+// of 32 samples), bytes past 4 wp = pad.
+int byte_slice_words(int wp);
+void launch_slice_bytes(const uint32_t* xs, int64_t n, int wp, int64_t rows, uint8_t pad, uint32_t* out,
+                        cudaStream_t s);
+// Whether the threshold-filter scan can serve C candidates over n points.
+bool byte_filter_plan(int64_t n, int C, int* stride, int* rank, int* cap);
+// Exact top-C keys [nq][C] by (byte Jaccard sketch distance, id): xsl_t the sliced base
+// tiled like the popcount scan's, xst the packed tiled base (listed rescans), qs packed
+// query rows [nq][wp].
+void launch_byte_filter_scan(const uint32_t* xsl_t, const uint32_t* xst, int64_t n, int wp, int sbytes,
+                             const uint32_t* qs, int nq, int C, uint64_t* out, cudaStream_t s);
+
 // ---- rerank.cu -------------------------------------------------------------------
 // Merge per-split sorted lists into one sorted list of C keys per query.
 void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t* out, cudaStream_t s);
+// Places of the FP64 re-check besides k (requests of smaller k answered from the same
+// launch); n <= 4.  Passed in device memory, so that a recorded launch can be replayed with
+// other places.
+struct RerankBounds {
+  int n;
+  int k[4];
+};
+
 // Exact re-rank of candidate keys (candidateSetScanner.cuh:10-32) and top-k output;
 // fp64_recheck: re-score, in double precision, the run of candidates around the k-th
 // place whose FP32 distances lie within the FP32 error bound of one another (among the
@@ -96,7 +118,7 @@ void launch_merge_splits(const uint64_t* in, int nq, int splits, int C, uint64_t
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d,
                    const float* xnorm, const float* q, const float* qnorm, int dist, int k,
                    struct ::lshg_point_s* out, cudaStream_t s, int* err = nullptr, bool fp64_recheck = false,
-                   const double* xn64 = nullptr);
+                   const double* xn64 = nullptr, const RerankBounds* extra_dev = nullptr);
 // Row norms in double precision (sum of squares in dimension order, then sqrt): the FP64
 // re-check's base magnitudes.
 void launch_row_norms_fp64(const float* x, int64_t n, int d, double* out, cudaStream_t s);

@@ -95,6 +95,7 @@ __device__ void fp64_boundary(uint64_t* keys, int C, int k, const float* __restr
   const int kk = imin(k, L) - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   if (kk < 0) return;
+  __syncthreads();  // a previous call's readers of s_lo / s_hi are done before they change
   if (threadIdx.x == 0) {
     auto joined = [&](int i) {  // entries i - 1 and i are within the band
       const uint64_t a = keys[i - 1], b = keys[i];
@@ -158,7 +159,7 @@ template <int DIST>
 __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                               int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
                               const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, float band_abs,
-                              float band_rel, const double* __restrict__ xn64) {
+                              float band_rel, const double* __restrict__ xn64, const RerankBounds* __restrict__ kx) {
   extern __shared__ __align__(16) unsigned char rsm[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(rsm);
   float* qr = reinterpret_cast<float*>(rsm + (size_t)C * 8);
@@ -180,7 +181,14 @@ __global__ void rerank_kernel(const uint64_t* __restrict__ cand, int nq, int C, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) {
+    fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+    const int nx = kx ? imin(kx->n, 4) : 0;
+    for (int b = 0; b < nx; ++b) {
+      const int kb = kx->k[b];
+      if (kb >= 1 && kb < k) fp64_boundary<DIST>(keys, C, kb, x, xn64, d, qr, band_abs, band_rel);
+    }
+  }
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -199,7 +207,8 @@ template <int DIST>
 __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, int C, const float* __restrict__ x,
                                      int64_t n, int d, const float* __restrict__ xnorm, const float* __restrict__ q,
                                      const float* __restrict__ qnorm, int k, lshg_point* __restrict__ out, int* err,
-                                     float band_abs, float band_rel, const double* __restrict__ xn64, int test_stall) {
+                                     float band_abs, float band_rel, const double* __restrict__ xn64, int test_stall,
+                                     const RerankBounds* __restrict__ kx) {
   extern __shared__ __align__(128) unsigned char rsm[];
   const int CH = blockDim.x;
   const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
@@ -271,7 +280,14 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
   }
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) {
+    fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+    const int nx = kx ? imin(kx->n, 4) : 0;
+    for (int b = 0; b < nx; ++b) {
+      const int kb = kx->k[b];
+      if (kb >= 1 && kb < k) fp64_boundary<DIST>(keys, C, kb, x, xn64, d, qr, band_abs, band_rel);
+    }
+  }
   for (int i = tid; i < k; i += CH) {
     const uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -352,7 +368,7 @@ __global__ void rerank_gather_kernel(const uint64_t* __restrict__ cand, int C, c
 template <int DIST>
 __global__ void rerank_select_kernel(const uint64_t* __restrict__ keys_in, int C, const float* __restrict__ x, int d,
                                      const float* __restrict__ q, int k, lshg_point* __restrict__ out, float band_abs,
-                                     float band_rel, const double* __restrict__ xn64) {
+                                     float band_rel, const double* __restrict__ xn64, const RerankBounds* __restrict__ kx) {
   extern __shared__ __align__(16) unsigned char rsm[];
   uint64_t* keys = reinterpret_cast<uint64_t*>(rsm);
   float* qr = reinterpret_cast<float*>(rsm + (size_t)C * 8);
@@ -361,7 +377,14 @@ __global__ void rerank_select_kernel(const uint64_t* __restrict__ keys_in, int C
   for (int i = threadIdx.x; i < C; i += blockDim.x) keys[i] = keys_in[(int64_t)qi * C + i];
   __syncthreads();
   block_bitonic_sort(keys, C);
-  if (band_abs >= 0.0f) fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+  if (band_abs >= 0.0f) {
+    fp64_boundary<DIST>(keys, C, k, x, xn64, d, qr, band_abs, band_rel);
+    const int nx = kx ? imin(kx->n, 4) : 0;
+    for (int b = 0; b < nx; ++b) {
+      const int kb = kx->k[b];
+      if (kb >= 1 && kb < k) fp64_boundary<DIST>(keys, C, kb, x, xn64, d, qr, band_abs, band_rel);
+    }
+  }
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     const uint64_t kk = i < C ? keys[i] : kEmptyKey;
     lshg_point pt;
@@ -414,10 +437,11 @@ void fp64_band(int dist, int d, float* band_abs, float* band_rel) {
 
 void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t n, int d, const float* xnorm,
                    const float* q, const float* qnorm, int dist, int k, lshg_point* out, cudaStream_t s, int* err,
-                   bool fp64_recheck, const double* xn64) {
+                   bool fp64_recheck, const double* xn64, const RerankBounds* extra_dev) {
   if (nq <= 0) return;
   float band_abs = -1.0f, band_rel = 0.0f;
   if (fp64_recheck) fp64_band(dist, d, &band_abs, &band_rel);
+  const RerankBounds* kb = extra_dev;  // further places of the FP64 re-check (device memory)
   // test hook: LSHG_TEST_ROW_WAIT_STALL=1 makes the first row-copy wait of the staged
   // re-rank run out (see rerank_staged_kernel)
   const char* stall_env = getenv("LSHG_TEST_ROW_WAIT_STALL");
@@ -442,7 +466,8 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
     LSHG_CHECK_LAUNCH();                                                                                        \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_select_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                    (int)select_smem));                                                          \
-    rerank_select_kernel<DV><<<nq, 512, select_smem, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel, xn64); \
+    rerank_select_kernel<DV><<<nq, 512, select_smem, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel, xn64, \
+                                                          kb);                                                \
   } while (0)
     switch (dist) {
       case DIST_ANGULAR: LSHG_RR2(DIST_ANGULAR); break;
@@ -462,7 +487,7 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
     LSHG_CUDA(cudaFuncSetAttribute(rerank_staged_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                    (int)staged_smem));                                                         \
     rerank_staged_kernel<DV><<<nq, CH, staged_smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, err, \
-                                                         band_abs, band_rel, xn64, test_stall);              \
+                                                         band_abs, band_rel, xn64, test_stall, kb);          \
   } while (0)
     switch (dist) {
       case DIST_ANGULAR: LSHG_RRS(DIST_ANGULAR); break;
@@ -483,7 +508,7 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
   do {                                                                                                    \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
     rerank_kernel<DV><<<nq, threads, smem, s>>>(cand, nq, C, x, n, d, xnorm, q, qnorm, k, out, band_abs,   \
-                                                band_rel, xn64);                                          \
+                                                band_rel, xn64, kb);                                      \
   } while (0)
   switch (dist) {
     case DIST_ANGULAR: LSHG_RR(DIST_ANGULAR); break;

@@ -284,9 +284,9 @@ int launch_scan_bits(const uint32_t* xs, int64_t n, int wp, int words, int sbyte
 
 // The queries list[1 .. list[0]] (a device-side list, at most nq of them) scanned over
 // the whole base, each result written to out[query][C]; blocks past the list's end exit.
-int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, const uint32_t* qs, int nq, int op,
-                            int C, const int* list, uint64_t* out, cudaStream_t s) {
-  return scan_bits_dispatch(xst, n, wp, words, 0, qs, nq, op, C, 1, out, list, s);
+int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq,
+                            int op, int C, const int* list, uint64_t* out, cudaStream_t s) {
+  return scan_bits_dispatch(xst, n, wp, words, sbytes, qs, nq, op, C, 1, out, list, s);
 }
 
 }  // namespace lshg

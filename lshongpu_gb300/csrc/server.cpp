@@ -12,9 +12,10 @@
 //    so that requests arriving meanwhile join it.  Requests with different k share a
 //    launch when the index computes the same candidates for them (batch_class): the
 //    launch runs at the largest k and each request receives the first k of its rows,
-//    which is its own top-k (the lists are sorted, ties by lower index; an index with the
-//    FP64 re-check, which orders the near-ties around the k-th place, shares a launch only
-//    between requests of equal k).  The batch is padded to a power-of-two
+//    which is its own top-k: the lists are sorted, ties by lower index, and the FP64
+//    re-check orders the near-ties around the k-th place of every k in the launch (at most
+//    four distinct k a launch; their list is copied to the device before each launch, so
+//    the recorded graph of the largest k serves every mix).  The batch is padded to a power-of-two
 //    class by repeating its last query, copied into the slot's pinned buffer and launched;
 //    requests that arrive while other batches are on the GPU go to the next free slot, so
 //    their work overlaps on the device;
@@ -22,8 +23,10 @@
 //    afterwards (falling back to direct launches if recording fails);
 //  * a host callback at the end of each slot's stream wakes the scheduler, which splits
 //    the results back into the requests and stamps their completion time.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <functional>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -65,12 +68,8 @@ struct Request {
 // buckets do not depend on k.
 int batch_class(const Index& I, int k) {
   const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
-  // tensor-core scans with the FP64 re-check order the near-ties around the k-th place,
-  // which depends on k: only requests with the same k share a launch
-  if (I.p.framework == 0 && (impl == 8 || impl == 9) && I.p.opt.fp64_recheck != 0) return 1 << 20 | k;
   if (I.p.framework == 0 && impl == 8) return k <= 32 ? 0 : 1;
   if (I.p.framework == 0 && impl == 9) return 0;  // 128 candidates at every k
-  if (I.p.framework == 0 && I.p.opt.fp64_recheck > 0) return 1 << 20 | k;
   int kp = 32;
   while (kp < k) kp <<= 1;
   const bool sketched = I.p.framework == 0 ? (impl >= 3 && impl <= 6) : (I.p.runWithSketchedData && I.sk_kind);
@@ -89,6 +88,8 @@ struct Slot {
   std::atomic<bool> finished{false};
   std::vector<std::shared_ptr<Request>> batch;
   int index_id = 0, k = 0, rows = 0;  // k: the launch's (largest) k
+  RerankBounds* h_ks = nullptr;       // the launch's smaller k (FP64 re-check places): pinned
+  RerankBounds* d_ks = nullptr;       // and device copies, read by the recorded launch
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;  // (index, k, class)
   std::map<std::tuple<int, int, int>, bool> no_graph;
 };
@@ -157,7 +158,7 @@ struct lshg_server {
         bool ok = cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
         if (ok) {
           try {
-            query_index(idx, s.d_in, rows_class, s.k, s.d_out, s.stream);
+            query_index(idx, s.d_in, rows_class, s.k, s.d_out, s.stream, s.d_ks);
           } catch (...) {
             ok = false;
           }
@@ -180,7 +181,7 @@ struct lshg_server {
         return;
       }
     }
-    query_index(idx, s.d_in, rows_class, s.k, s.d_out, s.stream);
+    query_index(idx, s.d_in, rows_class, s.k, s.d_out, s.stream, s.d_ks);
   }
 
   void launch(Slot& s, std::vector<std::shared_ptr<Request>>&& batch) {
@@ -204,9 +205,16 @@ struct lshg_server {
     s.index_id = s.batch[0]->index_id;
     s.k = kmax;
     s.rows = rows;
+    std::vector<int> kv;  // distinct k, largest first
+    for (auto& r : s.batch)
+      if (std::find(kv.begin(), kv.end(), r->k) == kv.end()) kv.push_back(r->k);
+    std::sort(kv.begin(), kv.end(), std::greater<int>());
+    *s.h_ks = RerankBounds{};
+    for (size_t i = 1; i < kv.size() && s.h_ks->n < 4; ++i) s.h_ks->k[s.h_ks->n++] = kv[i];
     s.busy = true;
     s.finished.store(false);
     LSHG_CUDA(cudaMemcpyAsync(s.d_in, s.h_in, (size_t)cls * d * sizeof(float), cudaMemcpyHostToDevice, s.stream));
+    LSHG_CUDA(cudaMemcpyAsync(s.d_ks, s.h_ks, sizeof(RerankBounds), cudaMemcpyHostToDevice, s.stream));
     run_batch(s, idx, cls);
     LSHG_CUDA(cudaMemcpyAsync(s.h_out, s.d_out, (size_t)rows * s.k * sizeof(lshg_point), cudaMemcpyDeviceToHost,
                               s.stream));
@@ -277,10 +285,13 @@ struct lshg_server {
       return {};
     }
     std::vector<std::shared_ptr<Request>> batch;
+    std::vector<int> kv;  // at most four distinct k a launch
     int rows = 0;
     for (auto it = queue.begin(); it != queue.end();) {
       auto& r = *it;
-      if (same(*r) && rows + r->nq <= p.max_batch) {
+      const bool newk = std::find(kv.begin(), kv.end(), r->k) == kv.end();
+      if (same(*r) && rows + r->nq <= p.max_batch && (!newk || kv.size() < 4)) {
+        if (newk) kv.push_back(r->k);
         rows += r->nq;
         r->state = 1;
         batch.push_back(r);
@@ -376,6 +387,9 @@ int lshg_server_create(const lshg_server_params* p, lshg_server** out) {
     for (int i = 0; i < s->p.streams; ++i) {
       auto sl = std::make_unique<Slot>();
       LSHG_CUDA(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
+      LSHG_CUDA(cudaMallocHost((void**)&sl->h_ks, sizeof(RerankBounds)));
+      LSHG_CUDA(cudaMalloc((void**)&sl->d_ks, sizeof(RerankBounds)));
+      *sl->h_ks = RerankBounds{};
       s->slots.push_back(std::move(sl));
     }
     s->worker = std::thread([s] { s->loop(); });
@@ -480,6 +494,8 @@ int lshg_server_destroy(lshg_server* s) {
     if (sl->d_in) cudaFree(sl->d_in);
     if (sl->h_out) cudaFreeHost(sl->h_out);
     if (sl->d_out) cudaFree(sl->d_out);
+    if (sl->h_ks) cudaFreeHost(sl->h_ks);
+    if (sl->d_ks) cudaFree(sl->d_ks);
     cudaStreamDestroy(sl->stream);
   }
   delete s;

@@ -71,6 +71,13 @@ void launch_expand_bits(const uint32_t* xs, int64_t n, int wp, int words, int64_
 // query sketches [nq][wp].  op: OP_HAMMING or OP_ONEBIT_JACCARD.
 void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int wp, int words, const uint32_t* qs,
                        int nq, int op, int C, uint64_t* out, int* err, cudaStream_t s);
+// Top-C keys [nq][C] of each query's survivors (keys make_key(-score, id), integer scores in
+// [-bits, bits]): a warp sort for C <= 128, a histogram of the scores and a sort of the
+// ties at the C-th score beyond; queries with fewer than `need` or more than `cap`
+// survivors (or too many ties) are listed in ovf and their rows left for a rescan.
+void launch_int_select(const int* cnt, const uint64_t* cand, int cap, int need, int C, int bits, int nq, uint64_t* out,
+                       int* ovf, cudaStream_t s);
+
 // Rows of kp bytes (a multiple of 16); boxes of 128 bytes x box_rows rows, 128-byte swizzle.
 CUtensorMap make_map_bytes(const void* base, int64_t rows, int kp, int box_rows);
 

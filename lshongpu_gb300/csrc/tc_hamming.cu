@@ -53,8 +53,8 @@
 
 namespace lshg {
 
-int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, const uint32_t* qs, int nq, int op,
-                            int C, const int* list, uint64_t* out, cudaStream_t s);
+int launch_scan_bits_listed(const uint32_t* xst, int64_t n, int wp, int words, int sbytes, const uint32_t* qs, int nq,
+                            int op, int C, const int* list, uint64_t* out, cudaStream_t s);
 
 namespace tc {
 
@@ -767,6 +767,21 @@ void launch_expand_bits(const uint32_t* xs, int64_t n, int wp, int words, int64_
   LSHG_CHECK_LAUNCH();
 }
 
+void launch_int_select(const int* cnt, const uint64_t* cand, int cap, int need, int C, int bits, int nq, uint64_t* out,
+                       int* ovf, cudaStream_t s) {
+  ProfScope _ps("tc_hamming_select", s);
+  LSHG_REQUIRE(bits >= 1 && 2 * bits + 1 <= H_BINS_MAX, "integer select: scores of at most 1024 bits");
+  if (C <= 128) {
+    if (C == 32) hsel_warp_kernel<1><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, need, nq, out, ovf);
+    else if (C == 64) hsel_warp_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, need, nq, out, ovf);
+    else hsel_warp_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt, cand, cap, need, nq, out, ovf);
+  } else {
+    hsel_hist_kernel<<<nq, 512, 0, s>>>(cnt, cand, cap, need, C, bits, out, ovf);
+  }
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+}
+
 void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int wp, int words, const uint32_t* qs,
                        int nq, int op, int C, uint64_t* out, int* err, cudaStream_t s) {
   if (nq <= 0) return;
@@ -817,21 +832,9 @@ void launch_tc_hamming(const uint8_t* xse, int64_t n, const uint32_t* xst, int w
   run_hamming_kc<MODE_FILTER, 64>(kc, ma, mb, a, "tc_hamming", s);
   DevBuf<int> ovf((size_t)nq + 1, s);
   LSHG_CUDA(cudaMemsetAsync(ovf.ptr, 0, sizeof(int), s));
-  const int need = (int)std::min<int64_t>(C, n);
-  {
-    ProfScope _ps("tc_hamming_select", s);
-    if (C <= 128) {
-      if (C == 32) hsel_warp_kernel<1><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
-      else if (C == 64) hsel_warp_kernel<2><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
-      else hsel_warp_kernel<4><<<ceil_div(nq, 8), 256, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, nq, out, ovf.ptr);
-    } else {
-      hsel_hist_kernel<<<nq, 512, 0, s>>>(cnt.ptr, cand.ptr, plan.cap, need, C, 32 * words, out, ovf.ptr);
-    }
-    count_launch();
-    LSHG_CHECK_LAUNCH();
-  }
+  launch_int_select(cnt.ptr, cand.ptr, plan.cap, (int)std::min<int64_t>(C, n), C, 32 * words, nq, out, ovf.ptr, s);
   // listed queries: exact popcount rescan written straight into their rows of `out`
-  launch_scan_bits_listed(xst, n, wp, words, qs, nq, op, C, ovf.ptr, out, s);
+  launch_scan_bits_listed(xst, n, wp, words, 0, qs, nq, op, C, ovf.ptr, out, s);
 }
 
 }  // namespace tc

@@ -526,7 +526,8 @@ void derive_tc(Index& I, cudaStream_t s) {
   launch_row_norms_fp64(I.x.ptr, I.n, I.d, I.xnorm64.ptr, s);
 }
 
-void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cudaStream_t s) {
+void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cudaStream_t s,
+                    const RerankBounds* extra) {
   using namespace tc;
   if (nq <= 0) return;
   LSHG_REQUIRE(k <= 128, "tensor-core scan: k must be <= 128");
@@ -599,7 +600,7 @@ void launch_tc_scan(Index& I, const float* q, int nq, int k, lshg_point* out, cu
   DevBuf<float> qn((size_t)nq, s);
   launch_row_norms(q, nq, I.d, qn.ptr, s);
   launch_rerank(best.ptr, nq, CT, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qn.ptr, DIST_ANGULAR, k, out, s, err,
-                I.p.opt.fp64_recheck != 0, I.xnorm64.ptr);
+                I.p.opt.fp64_recheck != 0, I.xnorm64.ptr, extra);
 }
 
 }  // namespace lshg

@@ -56,8 +56,9 @@ def test_same_alone_and_in_the_mix(engine, indexes):
 def test_batching_window_coalesces_requests(engine, indexes, which):
     """A burst of 40 requests (k from {10, 32, 100}) submitted within the 50 ms batching
     window is answered in at most one launch a candidate class (exact scan and LSH: one;
-    tensor-core scan with its FP64 re-check at the k-th place: one a k) -- far fewer
-    launches than requests -- and every request still equals its own query alone."""
+    tensor-core scan: k <= 32 and k > 32, its FP64 re-check ordering the near-ties at every
+    k of the launch) -- far fewer launches than requests -- and every request still equals
+    its own query alone."""
     x, idx = indexes
     rng = np.random.default_rng(7)
     srv = engine.Server(max_batch=4096, streams=2, use_graphs=True, batch_window_us=50_000)
@@ -74,8 +75,24 @@ def test_batching_window_coalesces_requests(engine, indexes, which):
         assert np.array_equal(out, idx[which].query(q, k))
     st = srv.stats()
     assert st["completed"] == len(reqs)
-    assert st["launches"] <= (3 if which == 3 else 1) + 2  # a burst split by the window at most once more
+    assert st["launches"] <= (2 if which == 3 else 1) + 2  # a burst split by the window at most once more
     assert st["launches"] < len(reqs) // 4
+    srv.close()
+
+
+def test_tensor_core_launch_with_several_k(engine, indexes):
+    """Requests of k = 10, 20, 32 and 5 on the tensor-core index coalesced into one launch
+    (the FP64 re-check then orders the near-ties at each of those places in turn): every
+    request equals its own query alone."""
+    x, idx = indexes
+    srv = engine.Server(max_batch=4096, streams=1, use_graphs=True, batch_window_us=50_000)
+    srv.add_index(3, idx[3])
+    reqs = [(datasets.clustered(64, D, 3000 + t, count=50), k) for t, k in enumerate((10, 20, 32, 5, 32, 10))]
+    tickets = [srv.submit(3, q, k) for q, k in reqs]
+    for (q, k), tk in zip(reqs, tickets):
+        out, _ = srv.wait(tk)
+        assert np.array_equal(out, idx[3].query(q, k)), k
+    assert srv.stats()["launches"] <= 3
     srv.close()
 
 

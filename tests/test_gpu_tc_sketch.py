@@ -94,3 +94,43 @@ def test_tc_and_popcount_paths_agree_by_default(engine):
                        options=engine.make_options(candidates=1024, sketch_scan=POPCOUNT))
     for qq in (q, q[:20]):
         assert np.array_equal(auto.query(qq, 32), pop.query(qq, 32))
+
+
+@pytest.mark.parametrize("C,n,S", [(256, 4000, 64), (4096, 60000, 256), (1024, 150000, 200)])
+def test_byte_minhash_filter_scan_matches_oracle(engine, orc, C, n, S):
+    """Byte weighted MinHash (implementation 4) through the threshold-filter scan: samples
+    bit-sliced, a histogram prepass on every S-th tile, survivors with at least tau equal
+    samples, the integer select; against the oracle's scan of the same sketches and its
+    generalized-Jaccard re-rank.  200 samples leave a partly padded group of 32."""
+    nq = 100
+    x = datasets.sparse_gamma(n, D, 33)
+    q = datasets.sparse_gamma(nq, D, 34)
+    idx = engine.Index(x, implementation=4, distanceFunc=2, sketchDim=S,
+                       options=engine.make_options(candidates=C, sketch_scan=TENSOR))
+    xp = np.frombuffer(idx.export(engine.EXPORT_DATA), np.float32).reshape(n, D)
+    skx = np.frombuffer(idx.export(engine.EXPORT_SKETCHES), np.uint8).reshape(n, S)
+    skq, _ = idx.sketch_queries(q, np.uint8, S)
+    res = idx.query(q, 32)
+    ids, ds = orc.sketch_scan(xp, orc.normalize(q), 4, skx, skq, S, C, 2, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
+
+
+def test_byte_minhash_filter_ties_rescanned(engine, orc):
+    """A third of the base is one duplicated row: queries equal to it tie with every copy
+    at the top match count, overflow the candidate arrays and are rescanned; all equal the
+    oracle."""
+    n, nq, S, C = 45000, 80, 64, 512
+    x = datasets.sparse_gamma(n, D, 35)
+    x[::3] = x[0]
+    q = datasets.sparse_gamma(nq, D, 36)
+    q[:20] = x[0]
+    idx = engine.Index(x, implementation=4, distanceFunc=2, sketchDim=S,
+                       options=engine.make_options(candidates=C, sketch_scan=TENSOR))
+    xp = np.frombuffer(idx.export(engine.EXPORT_DATA), np.float32).reshape(n, D)
+    skx = np.frombuffer(idx.export(engine.EXPORT_SKETCHES), np.uint8).reshape(n, S)
+    skq, _ = idx.sketch_queries(q, np.uint8, S)
+    res = idx.query(q, 32)
+    ids, ds = orc.sketch_scan(xp, orc.normalize(q), 4, skx, skq, S, C, 2, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
