@@ -172,6 +172,8 @@ def build_index(L, x, path: str):
 FP32_SIMT_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # 32-bit population count: 16 a clock an SM (nominal), 152 SMs at 2.07 GHz, in G word/s
 POPC_NOMINAL_GWORDS = 152 * 16 * 2.07e9 / 1e9
+# integer ALU pipe (logic operations): 64 lanes a clock an SM, in G operations/s
+ALU_NOMINAL_GOPS = 152 * 64 * 2.07e9 / 1e9
 
 
 def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
@@ -191,6 +193,11 @@ def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
     if path in ("simhash", "wmh1") and "tc_hamming" in prof:
         bits = 1024 if path == "simhash" else 256
         return "tc_hamming", "tensor8", 2.0 * nq * N_BASE * bits / 1e12, "TFLOP/s"
+    # byte samples through the bit-sliced threshold filter: every (query, point) pair
+    # compares 8 bit-plane words a group of 32 samples, one three-input logic operation a
+    # word on the integer ALU pipe; work = Q x N x 64 plane words (256 samples)
+    if path == "wmh" and "scan_bytes_filter" in prof:
+        return "scan_bytes_filter", "alu", nq * N_BASE * 64 / 1e9, "Gword/s"
     # sketch scans on the popcount path are integer-bound at these batch sizes: work = sketch
     # words compared (one XOR + POPC each, zero-byte count for byte samples), Q x N x words
     if path == "simhash":
@@ -546,6 +553,8 @@ def main():
         peak, peak_kind = 2 * bf16, "2 x measured bf16 (dense FP8 rate = 2 x BF16)"
     elif bound == "popc":
         peak, peak_kind = POPC_NOMINAL_GWORDS, "nominal (152 SMs x 16 popc/clk x 2.07 GHz)"
+    elif bound == "alu":
+        peak, peak_kind = ALU_NOMINAL_GOPS, "nominal (152 SMs x 64 integer ALU lanes/clk x 2.07 GHz)"
     else:
         peak = None
     traffic = dram_traffic(kname, workload_text(args))

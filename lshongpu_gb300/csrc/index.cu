@@ -615,7 +615,7 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
         byte_filter_plan(I.n, C, &fs, &fr, &fc)) {
       // byte samples: bit-sliced threshold filter, the exact top-C, then the same re-rank
       part.alloc((size_t)nq * C, s);
-      launch_byte_filter_scan(I.xsl.ptr, I.xst.ptr, I.n, I.wp, I.sbytes, qs.ptr, nq, C, part.ptr, s);
+      launch_byte_filter_scan(I.xsl.ptr, I.xst.ptr, I.n, I.wp, I.sbytes, qs.ptr, nq, C, part.ptr, I.error_word(s), s);
       launch_rerank(part.ptr, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
                     I.p.opt.fp64_recheck > 0, nullptr, extra);
       return;

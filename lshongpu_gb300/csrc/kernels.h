@@ -98,7 +98,7 @@ bool byte_filter_plan(int64_t n, int C, int* stride, int* rank, int* cap);
 // tiled like the popcount scan's, xst the packed tiled base (listed rescans), qs packed
 // query rows [nq][wp].
 void launch_byte_filter_scan(const uint32_t* xsl_t, const uint32_t* xst, int64_t n, int wp, int sbytes,
-                             const uint32_t* qs, int nq, int C, uint64_t* out, cudaStream_t s);
+                             const uint32_t* qs, int nq, int C, uint64_t* out, int* err, cudaStream_t s);
 
 // ---- rerank.cu -------------------------------------------------------------------
 // Merge per-split sorted lists into one sorted list of C keys per query.
