@@ -70,6 +70,7 @@ CONFIGS = {
     "4a-l48": dict(path="cplsh", N_BASE=1_000_000, PAD_DIM=28, CP_HASHES=2, CP_TABLES=48),
     "4b": dict(path="wmh", N_BASE=500_000, DATA="sparse"),
     "4b-1bit": dict(path="wmh1", N_BASE=500_000, DATA="sparse"),
+    "4b-cws": dict(path="cws", N_BASE=500_000, DATA="sparse"),
 }
 
 
@@ -165,6 +166,8 @@ def build_index(L, x, path: str):
         return L.Index(x, implementation=4, distanceFunc=2, sketchDim=256)
     if path == "wmh1":
         return L.Index(x, implementation=5, distanceFunc=2, sketchDim=8)
+    if path == "cws":
+        return L.Index(x, implementation=L.IMPL_CWS, distanceFunc=2, sketchDim=256)
     raise SystemExit(f"unknown path {path}")
 
 
@@ -198,6 +201,10 @@ def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
     # word on the integer ALU pipe; work = Q x N x 64 plane words (256 samples)
     if path == "wmh" and "scan_bytes_filter" in prof:
         return "scan_bytes_filter", "alu", nq * N_BASE * 64 / 1e9, "Gword/s"
+    # CWS codes through the same filter: 16 bit planes a 32-sample group, 128 plane words a
+    # pair at 256 samples
+    if path == "cws":
+        return "scan_cws", "alu", nq * N_BASE * 128 / 1e9, "Gword/s"
     # sketch scans on the popcount path are integer-bound at these batch sizes: work = sketch
     # words compared (one XOR + POPC each, zero-byte count for byte samples), Q x N x words
     if path == "simhash":
@@ -352,7 +359,9 @@ def workload_text(args) -> str:
             "simhash": f"1024-bit SimHash, {CAND} candidates re-ranked",
             "cplsh": f"cross-polytope LSH, L={CP_TABLES}, K={CP_HASHES}, 3 rounds, exact angular on candidates",
             "wmh": "weighted MinHash, 256 byte samples, Jaccard scan + generalized-Jaccard re-rank",
-            "wmh1": "weighted MinHash, 256 one-bit samples, Jaccard scan + generalized-Jaccard re-rank"}[args.path]
+            "wmh1": "weighted MinHash, 256 one-bit samples, Jaccard scan + generalized-Jaccard re-rank",
+            "cws": "consistent weighted sampling, 256 (index, int32) samples, exact match counts + "
+                   "generalized-Jaccard re-rank"}[args.path]
     cfg = f"configuration {args.config}: " if args.config else ""
     return f"{cfg}{what}: N={N_BASE}, d={d}, Q={N_QUERY}, k={K}, {data}"
 
@@ -398,7 +407,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--path", default=None, choices=["tc", "tc8", "exact", "simhash", "cplsh", "wmh", "wmh1"])
+    ap.add_argument("--path", default=None, choices=["tc", "tc8", "exact", "simhash", "cplsh", "wmh", "wmh1", "cws"])
     ap.add_argument("--config", default=None, choices=sorted(CONFIGS), help="measurement configuration")
     ap.add_argument("--no-extras", action="store_true", help="skip recall / baselines / serving extras")
     ap.add_argument("--n", type=int, default=None, help="base size (profiling cases only)")
@@ -660,7 +669,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
-        "dtype": ({"tc": "bf16", "tc8": "e4m3", "wmh": "u8"}.get(args.path)
+        "dtype": ({"tc": "bf16", "tc8": "e4m3", "wmh": "u8", "cws": "int32 pairs (u16 codes)"}.get(args.path)
               or ("e4m3 (+-1 sketch bits)" if "tc_hamming" in prof else None)
               or {"simhash": "u32", "wmh1": "u32"}.get(args.path, "f32")),
         "data": "synthetic",

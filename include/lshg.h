@@ -25,7 +25,12 @@
  *                            6 = Johnson-Lindenstrauss,
  *                            8 = tensor-core exact scan (BF16, no reference counterpart),
  *                            9 = the same with E4M3 (FP8) tensor-core scores; both
- *                                return exact FP32 distances of their candidates
+ *                                return exact FP32 distances of their candidates,
+ *                            10 = consistent weighted sampling (Ioffe's ICWS; no
+ *                                reference counterpart): sketchDim (index, t) samples,
+ *                                a multiple of 32 up to 256, linear scan only, the
+ *                                weighted MinHash preprocessing and generalized-Jaccard
+ *                                re-rank
  *   keysImplementation:  3 = SimHash, 4 = WMH byte, 5 = one-bit WMH, 7 = cross-polytope
  *   distanceFunc:        1 = angular, 2 = generalized Jaccard, 3 = Euclidean
  */
@@ -193,13 +198,17 @@ int lshg_index_query_noalloc(lshg_index* idx, const float* d_queries, int N_quer
 
 /* Export index internals to host memory for checks and persistence.  what:
  *  0 = base data after preprocessing (float [n][d])
- *  1 = sketches (u32 words [n][sketchDim] for 3/5, u8 [n][sketchDim] for 4, float for 6)
+ *  1 = sketches (u32 words [n][sketchDim] for 3/5, u8 [n][sketchDim] for 4, float for 6,
+ *      int32 (index, t) pairs [n][sketchDim][2] for 10)
  *  2 = LSH keys (u16 [n][tables])
  *  3 = LSH bucket offsets (int32 [tables][tableSize], absolute into the bucket array)
  *  4 = LSH bucket ids (int32 [tables][n], ascending ids within each bucket)
  *  5 = query counters (uint64 [2], cumulative since the build or load: LSH bucket
  *      entries walked, distinct LSH candidates scored); read after the queries' streams
  *      have been synchronised
+ *  6 = consistent-weighted-sampling code plan (int32 [5]: min and max t over the base's
+ *      samples, code bits of the dimension index and of t, bit planes of the sliced codes
+ *      -- 8 or 16, 0 when the codes need more than 16 bits and every scan is direct)
  * If dst is NULL only *bytes is set. */
 int lshg_index_export(lshg_index* idx, int what, void* dst, size_t* bytes);
 /* Hash/sketch queries with the index's random vectors: sketches and keys as in export. */

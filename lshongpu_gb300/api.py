@@ -30,6 +30,7 @@ IMPL_WMH_ONEBIT = 5
 IMPL_JL = 6
 IMPL_TC = 8
 IMPL_TC_FP8 = 9
+IMPL_CWS = 10  # consistent weighted sampling (no reference counterpart)
 # keysImplementation codes (kernel.cu:65-85)
 KEYS_SIMHASH = 3
 KEYS_WMH = 4
@@ -176,6 +177,7 @@ def random_bools(count: int) -> np.ndarray:
 # ---- resident index ----------------------------------------------------------------
 
 EXPORT_DATA, EXPORT_SKETCHES, EXPORT_KEYS, EXPORT_OFFSETS, EXPORT_BUCKETS = 0, 1, 2, 3, 4
+EXPORT_QUERY_COUNTERS, EXPORT_CWS_CODES = 5, 6
 
 
 class Index:
@@ -388,8 +390,8 @@ __all__ = [
     "POINT_DTYPE", "Result", "LshgError", "calculate_k", "linear_scans", "LSH", "lsh", "random_normals",
     "random_plus_minus", "random_bools", "Index", "merge_topk", "validate", "parse_file", "write_file", "Server",
     "make_options", "launch_count", "profile_enable", "profile_report", "IMPL_EXACT", "IMPL_SIMHASH", "IMPL_WMH",
-    "IMPL_WMH_ONEBIT", "IMPL_JL", "IMPL_TC", "IMPL_TC_FP8", "KEYS_SIMHASH", "KEYS_WMH", "KEYS_WMH_ONEBIT", "KEYS_CROSSPOLY",
+    "IMPL_WMH_ONEBIT", "IMPL_JL", "IMPL_TC", "IMPL_TC_FP8", "IMPL_CWS", "KEYS_SIMHASH", "KEYS_WMH", "KEYS_WMH_ONEBIT", "KEYS_CROSSPOLY",
     "SKETCH_SCAN_AUTO", "SKETCH_SCAN_POPCOUNT", "SKETCH_SCAN_TENSOR",
     "ANGULAR", "JACCARD", "EUCLIDEAN", "EXPORT_DATA", "EXPORT_SKETCHES", "EXPORT_KEYS", "EXPORT_OFFSETS",
-    "EXPORT_BUCKETS", "POINT_DTYPE", "read_truth", "write_truth",
+    "EXPORT_BUCKETS", "EXPORT_QUERY_COUNTERS", "EXPORT_CWS_CODES", "POINT_DTYPE", "read_truth", "write_truth",
 ]

@@ -40,6 +40,16 @@ void tile_sketches(Index& I, cudaStream_t s) {
     I.xsl.alloc((size_t)tiles * 128 * wsl, s);
     launch_tile_sketches(sl.ptr, I.n, wsl, I.xsl.ptr, s);
   }
+  if (I.sk_kind == 10) {  // CWS: codes against the base's range of t, bit-sliced for the filter scan
+    I.cws = cws_plan_codes(I.xs.ptr, I.n, I.cws_S, I.d, s);
+    if (I.cws.pl && I.p.opt.sketch_scan != 1) {
+      const int wsl = I.cws_S / 32 * I.cws.pl;
+      DevBuf<uint32_t> sl((size_t)I.n * wsl, s);
+      launch_cws_slice(I.xs.ptr, I.n, I.cws_S, I.d, I.cws, false, sl.ptr, s);
+      I.xsl.alloc((size_t)tiles * 128 * wsl, s);
+      launch_tile_sketches(sl.ptr, I.n, wsl, I.xsl.ptr, s);
+    }
+  }
   if ((I.sk_kind == 3 || I.sk_kind == 5) && I.words <= 32 && I.p.opt.sketch_scan != 1) {
     const int64_t rows = (I.n + 255) / 256 * 256;
     I.xse.alloc((size_t)rows * 128 * tc::hamming_chunks(I.words), s);
@@ -197,6 +207,11 @@ void make_sketch(const Index& idx, const float* v, int64_t rows, uint8_t padbyte
       launch_pad_words(raw.ptr, rows, idx.words, packed->ptr, idx.wp, 0u, s);
       break;
     }
+    case 10: {
+      packed->alloc(rows * idx.wp, s);
+      launch_cws_sketch(v, rows, d, idx.cws_S, idx.cws_tab.ptr, packed->ptr, s);
+      break;
+    }
     case 6: {
       fl->alloc(rows * idx.sdim, s);
       launch_project(v, rows, d, idx.sk_planes.ptr, idx.sdim, 1, 32, 0, nullptr, fl->ptr, s);
@@ -301,6 +316,7 @@ Index::~Index() {
   sk_planes.release(); sk_split.release(); sk_pnorm.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
   xbf.release(); xbf_scale.release(); xf8.release(); xnorm64.release(); xst.release(); qstats.release();
+  cws_tab.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();
@@ -337,7 +353,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
   double prep = 0, build = 0;
   float* X = I.x.ptr;
 
-  LSHG_REQUIRE(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8 || impl == 9,
+  LSHG_REQUIRE(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8 || impl == 9 || impl == 10,
                "Invalid implementation selected");
   LSHG_REQUIRE(p.framework == 0 || p.framework == 1, "framework must be 0 (linear scan) or 1 (LSH)");
 
@@ -360,6 +376,11 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
       case 5:
         I.dist = DIST_JACCARD;  // weightedMinHash.cuh:28
         break;
+      case 10:  // the weighted MinHash preprocessing (processingUtils.cuh:12-67), then CWS samples
+        I.dist = DIST_JACCARD;
+        do_shift(I.ops_sketch, X, n, comp, nc, d, s);
+        do_normalize(I.ops_sketch, X, n, comp, nc, d, s);
+        break;
       case 6:
         I.dist = DIST_ANGULAR;  // candidateSetScan(..., 1), sketchedDistanceScanners.cuh:168
         do_normalize(I.ops_sketch, X, n, comp, nc, d, s);  // simHashJL.cuh:298
@@ -369,6 +390,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
     I.dist = p.distanceFunc;
     LSHG_REQUIRE(I.dist >= 1 && I.dist <= 3, "Invalid operation selected for distance function");
     LSHG_REQUIRE(impl != 8 && impl != 9, "the tensor-core scan is a linear scan");
+    LSHG_REQUIRE(impl != 10, "consistent weighted sampling is a linear-scan sketch");
     LSHG_REQUIRE(p.tables >= 1 && p.tables <= 256, "tables must be in [1, 256]");
     LSHG_REQUIRE(p.bucketKeyBits >= 1 && p.bucketKeyBits <= 24, "bucketKeyBits must be in [1, 24]");
     I.tables = p.tables;
@@ -421,7 +443,7 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
   }
 
   // sketches (generateHashes(isHashKeys = false), lshFramework.cuh:391)
-  const bool want_sketch = (p.framework == 0) ? (impl >= 3 && impl <= 6) : (impl >= 3 && impl <= 6);
+  const bool want_sketch = (impl >= 3 && impl <= 6) || (p.framework == 0 && impl == 10);
   if (want_sketch) {
     LSHG_REQUIRE(p.sketchDim >= 1, "sketchDim must be >= 1");
     I.sk_kind = impl;
@@ -449,6 +471,18 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
         LSHG_REQUIRE(I.wp <= 64, "one-bit weighted-MinHash sketchDim must be <= 64 words");
         wmh_prepare(I.wmh_sk, I.ops_sketch, X, n, comp, nc, d, p.sketchDim * 32, 1, p.sketchDim, 32, s);
         break;
+      case 10: {
+        LSHG_REQUIRE(p.sketchDim >= 32 && p.sketchDim <= 256 && p.sketchDim % 32 == 0,
+                     "CWS sketchDim (samples) must be a multiple of 32 in [32, 256]");
+        LSHG_REQUIRE(d <= 4096, "CWS: d must be <= 4096");
+        I.cws_S = p.sketchDim;
+        I.words = 2 * p.sketchDim;
+        I.wp = I.words;
+        std::vector<float> tab;
+        cws_tables(d, I.cws_S, tab);
+        upload(I.cws_tab, tab.data(), tab.size(), s);
+        break;
+      }
       case 6: {
         I.sdim = p.sketchDim;
         if (p.framework == 1) do_normalize(I.ops_sketch, X, n, comp, nc, d, s);  // runGenericJL, simHashJL.cuh:254
@@ -595,6 +629,14 @@ void query_index(Index& I, float* q, int nq, int k, lshg_point* out, cudaStream_
   const int C = std::max(I.C, kp);
   DevBuf<uint64_t> part;
   int splits;
+  if (impl == 10) {  // CWS: the exact top-C by (1 - matches / S, id), then the generalized-Jaccard re-rank
+    part.alloc((size_t)nq * C, s);
+    launch_cws_scan(I.cws.pl ? I.xsl.ptr : nullptr, I.xst.ptr, I.n, I.cws_S, I.d, I.cws, qs.ptr, nq, C, part.ptr,
+                    I.error_word(s), s);
+    launch_rerank(part.ptr, nq, C, I.x.ptr, I.n, I.d, I.xnorm.ptr, q, qnorm.ptr, I.dist, k, out, s, I.error_word(s),
+                  I.p.opt.fp64_recheck > 0, nullptr, extra);
+    return;
+  }
   if (impl == 6) {
     splits = scan_float_splits(I.n, nq, C);
     part.alloc((size_t)nq * splits * C, s);

@@ -51,13 +51,13 @@ struct Index {
   std::vector<PrepOp> ops_keys;    // applied before keys are computed
   std::vector<PrepOp> ops_sketch;  // applied after keys, before sketches
 
-  // sketches: kind 0 none, 3 SimHash, 4 byte WMH, 5 one-bit WMH, 6 JL
+  // sketches: kind 0 none, 3 SimHash, 4 byte WMH, 5 one-bit WMH, 6 JL, 10 CWS
   int sk_kind = 0;
   int words = 0, wp = 0, sbytes = 0, sdim = 0;
   DevBuf<uint32_t> xs;       // packed sketches, rows of wp words
   DevBuf<uint32_t> xst;      // linear scans: the same, tiled [ceil(N/128)][wp/4][128] x 16 B
-  DevBuf<uint32_t> xsl;      // byte samples bit-sliced and tiled like xst, for the threshold-filter
-                             // scan (derived, not stored)
+  DevBuf<uint32_t> xsl;      // byte samples (kind 4) or CWS codes (kind 10) bit-sliced and tiled
+                             // like xst, for the threshold-filter scan (derived, not stored)
   DevBuf<uint8_t> xse;       // tensor-core sketch scans: sketch bits as E4M3 +-1 rows,
                              // [ceil(n/256)*256][128 * ceil(words/4)] (derived, not stored)
   DevBuf<float> xsf, xsft;   // JL sketches [n][sdim] and their tile layout
@@ -66,6 +66,9 @@ struct Index {
                              // tensor-core projection (d <= 128; derived, not stored)
   DevBuf<float> sk_pnorm;    // their norms, rows padded to 256
   WmhState wmh_sk;
+  int cws_S = 0;             // CWS samples a vector; xs rows are S (index, t) int32 pairs
+  DevBuf<float> cws_tab;     // CWS draw table [d][S][4]
+  CwsCodes cws;              // CWS code plan (derived from xs at build and at load)
 
   // LSH
   int key_kind = 0;

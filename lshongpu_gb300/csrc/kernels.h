@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace lshg {
 
 // Distance-function codes of the reference (distanceFunctions.cuh:54-71) plus the
@@ -99,6 +101,28 @@ bool byte_filter_plan(int64_t n, int C, int* stride, int* rank, int* cap);
 // query rows [nq][wp].
 void launch_byte_filter_scan(const uint32_t* xsl_t, const uint32_t* xst, int64_t n, int wp, int sbytes,
                              const uint32_t* qs, int nq, int C, uint64_t* out, int* err, cudaStream_t s);
+
+// Consistent weighted sampling (implementation 10, cws.cu): (index, t) samples of the
+// generalized Jaccard similarity, their range-coded bit-sliced form, and the scan.
+constexpr uint64_t kCwsSeed = 0x6C7368672D637773ull;
+struct CwsCodes {
+  int tmin = 0, tmax = 0;  // range of t over the base's samples
+  int kb = 0, tb = 0;      // code bits of the dimension index and of t - tmin
+  int pl = 0;              // bit planes of the sliced codes (8 or 16); 0: codes need more than 16 bits
+};
+// Draw table [d][S] of (r, 1/r, ln c, beta) as 4 floats.
+void cws_tables(int d, int S, std::vector<float>& tab);
+// Samples of `rows` vectors: rows of S (index, t) int32 pairs (2 S words).
+void launch_cws_sketch(const float* x, int64_t rows, int d, int S, const float* tab, uint32_t* out, cudaStream_t s);
+// Code plan from the base's samples (synchronises the stream to read their range of t).
+CwsCodes cws_plan_codes(const uint32_t* xs, int64_t n, int S, int d, cudaStream_t s);
+// Samples -> codes bit-sliced into rows of (S / 32) * pl words (queries: padding never matches).
+void launch_cws_slice(const uint32_t* smp, int64_t rows, int S, int d, const CwsCodes& c, bool query, uint32_t* out,
+                      cudaStream_t s);
+// Exact top-C by (1 - matches / S, id) of every query into out [nq][C].  xsl_t: the base's
+// tiled sliced codes (nullptr when c.pl == 0); xst: its samples tiled [tile][S / 2][128].
+void launch_cws_scan(const uint32_t* xsl_t, const uint32_t* xst, int64_t n, int S, int d, const CwsCodes& c,
+                     const uint32_t* qs, int nq, int C, uint64_t* out, int* err, cudaStream_t s);
 
 // ---- rerank.cu -------------------------------------------------------------------
 // Merge per-split sorted lists into one sorted list of C keys per query.

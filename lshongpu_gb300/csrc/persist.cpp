@@ -22,7 +22,7 @@ void set_last_error(const char* msg);
 
 namespace {
 
-constexpr char kMagic[8] = {'L', 'S', 'H', 'G', 'I', 'D', 'X', '3'};
+constexpr char kMagic[8] = {'L', 'S', 'H', 'G', 'I', 'D', 'X', '4'};
 
 struct Writer {
   FILE* f;
@@ -111,6 +111,7 @@ void scalars(IO& io, IdxT& I) {
   io.pod(I.wp);
   io.pod(I.sbytes);
   io.pod(I.sdim);
+  io.pod(I.cws_S);
   io.pod(I.key_kind);
   io.pod(I.tableSize);
   io.pod(I.tables);
@@ -192,14 +193,16 @@ void check_loaded(const Reader& r, const Index& I) {
   need(n >= 1 && n < (int64_t)INT_MAX && d >= 1 && d <= (1 << 16) && I.p.d == d, "base size");
   need(I.p.framework == 0 || I.p.framework == 1, "framework");
   const int impl = I.p.implementation == 1 ? 2 : I.p.implementation;
-  need(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8 || impl == 9, "implementation");
+  need(impl == 2 || impl == 3 || impl == 4 || impl == 5 || impl == 6 || impl == 8 || impl == 9 || impl == 10,
+       "implementation");
+  need(impl != 10 || I.p.framework == 0, "implementation");
   need(I.dist >= 1 && I.dist <= 3, "distance function");
   need(I.C >= 32 && I.C <= 4096 && (I.C & (I.C - 1)) == 0, "candidate count");
   const size_t tiles = (size_t)ceil_div(n, 128);
   need(r.count(&I.x) == (size_t)n * d, "base rows");
   need(r.count(&I.xnorm) == (I.dist == DIST_ANGULAR ? (size_t)n : 0), "magnitudes");
   need(r.count(&I.xt) == (I.p.framework == 0 && impl == 2 ? tiles * 128 * d : 0), "base tiles");
-  const bool sketched = impl >= 3 && impl <= 6;
+  const bool sketched = (impl >= 3 && impl <= 6) || impl == 10;
   need(I.sk_kind == (sketched ? impl : 0), "sketch kind");
   size_t xs = 0, xsf = 0, xsft = 0, planes = 0;
   switch (I.sk_kind) {
@@ -219,6 +222,12 @@ void check_loaded(const Reader& r, const Index& I) {
       xs = (size_t)n * I.wp;
       check_wmh(r, I.wmh_sk, d, I.words * 32, 1, I.words, 32);
       break;
+    case 10:
+      need(I.cws_S >= 32 && I.cws_S <= 256 && I.cws_S % 32 == 0 && I.words == 2 * I.cws_S && I.wp == I.words &&
+               d <= 4096,
+           "CWS width");
+      xs = (size_t)n * I.wp;
+      break;
     case 6:
       need(I.sdim >= 1 && I.sdim <= (1 << 16), "JL width");
       xsf = (size_t)n * I.sdim;
@@ -227,6 +236,7 @@ void check_loaded(const Reader& r, const Index& I) {
       break;
   }
   if (I.sk_kind != 4 && I.sk_kind != 5) check_no_wmh(r, I.wmh_sk);
+  need(r.count(&I.cws_tab) == (I.sk_kind == 10 ? (size_t)d * I.cws_S * 4 : 0), "CWS draw table");
   need(r.count(&I.xs) == xs && r.count(&I.xsf) == xsf && r.count(&I.xsft) == xsft && r.count(&I.sk_planes) == planes,
        "sketch buffers");
   if (I.p.framework == 1) {
@@ -334,6 +344,7 @@ void buffers_io(IO& io, Index& I, cudaStream_t s) {
   io.dev(I.xbf, s);
   io.dev(I.xbf_scale, s);
   io.dev(I.xf8, s);
+  io.dev(I.cws_tab, s);
   wmh_io(io, I.wmh_sk, s);
   wmh_io(io, I.wmh_keys, s);
 }

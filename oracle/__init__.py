@@ -32,6 +32,9 @@ _SIGS = {
     "or_crosspoly": (None, [P, i64, i32, i32, i32, i32, i32, P, P]),
     "or_wmh_bounds": (i32, [P, i64, P, i64, i32, P, P, i32]),
     "or_wmh_sketch": (i64, [P, i64, i32, P, P, i32, P, i32, i32, i32, i32, i32, P, i32, P, P]),
+    "or_cws_tables": (None, [i32, i32, P]),
+    "or_cws_logf": (C.c_float, [C.c_float]),
+    "or_cws_sketch": (None, [P, i64, i32, i32, P, P]),
     "or_sketch_scan": (None, [P, i64, P, i64, i32, i32, P, P, i32, i32, i32, i32, P, P, P]),
     "or_lsh_build": (None, [P, i64, i32, i32, P, P]),
     "or_lsh_query": (None, [P, i64, P, i64, i32, P, i32, i32, P, P, i32, i32, P, P, i32, i32, i32, i32, P, P]),
@@ -161,6 +164,27 @@ def wmh_sketch(x, start, mp, M, u, H, T, onebit, words, hashBits, bitmap):
                                _p(np.ascontiguousarray(mp, np.int32)), M, _p(u), H, T, int(onebit), words, hashBits,
                                _p(bitmap), len(bitmap), _p(out8), _p(out32))
     return (out32 if onebit else out8), int(over)
+
+
+def cws_tables(d, S):
+    """Consistent weighted sampling draw table [d][S][4]: r, 1/r, ln c, beta."""
+    out = np.empty((d, S, 4), np.float32)
+    lib().or_cws_tables(d, S, _p(out))
+    return out
+
+
+def cws_logf(x):
+    return np.float32(lib().or_cws_logf(C.c_float(float(x))))
+
+
+def cws_sketch(x, S, tab=None):
+    """(index, t) samples [n][S][2] int32 of nonnegative rows x (after preprocessing)."""
+    x = _f32(x)
+    n, d = x.shape
+    tab = cws_tables(d, S) if tab is None else np.ascontiguousarray(tab, np.float32)
+    out = np.empty((n, S, 2), np.int32)
+    lib().or_cws_sketch(_p(x), n, d, S, _p(tab), _p(out))
+    return out
 
 
 def sketch_scan(x, q, kind, xs, qs, width, C_, dist, k, want_cand=False):

@@ -421,11 +421,121 @@ int64_t or_wmh_sketch(const float* x, int64_t n, int d, const int32_t* start, co
 }
 
 /* ---------------------------------------------------------------------------
+ * Consistent weighted sampling (implementation 10; no reference counterpart).
+ * Restates the engine's sketch (lshongpu_gb300/csrc/cws.cu) from the published
+ * algorithm -- Ioffe, "Improved Consistent Sampling, Weighted Minhash and L1
+ * Sketching", ICDM 2010 -- with the engine's draw table and single-precision steps:
+ *   t_i = floor(ln S_i * (1/r) + beta),  ln a_i = ln c - r ((t_i - beta) + 1),
+ *   sample = (argmin_i ln a_i (lowest i on ties), t_i*), (d, 0) for no positive entry.
+ * Draws: splitmix64 (Steele, Lea, Flood, OOPSLA 2014) as a counter hash.  This file is
+ * built with -ffp-contract=off, so each float operation below is rounded on its own, as
+ * the device code's __f*_rn intrinsics are.
+ * ------------------------------------------------------------------------- */
+#define CWS_SEED 0x6C7368672D637773ull
+
+static uint64_t cws_mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static double cws_uniform(int j, int i, int m) {
+  uint64_t c = ((uint64_t)j * 65536u + (uint64_t)i) * 8u + (uint64_t)m;
+  uint64_t z = cws_mix(CWS_SEED + (c + 1) * 0x9E3779B97F4A7C15ull);
+  return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+/* table [d][S][4]: r, 1/r, ln c, beta (r, c ~ Gamma(2, 1) as sums of two Exp(1)) */
+void or_cws_tables(int d, int S, float* tab) {
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < S; ++j) {
+      double r = -(log(cws_uniform(j, i, 0)) + log(cws_uniform(j, i, 1)));
+      double c = -(log(cws_uniform(j, i, 2)) + log(cws_uniform(j, i, 3)));
+      float rf = (float)r;
+      float* t = tab + ((size_t)i * S + j) * 4;
+      t[0] = rf;
+      t[1] = 1.0f / rf;
+      t[2] = (float)log(c);
+      t[3] = (float)cws_uniform(j, i, 4);
+    }
+}
+
+/* ln x for positive finite x: x = m 2^e, m in [sqrt(1/2), sqrt(2)], ln m = 2 atanh(s),
+ * s = (m - 1)/(m + 1), the atanh series to s^9, ln2 split in a high and a low part. */
+float or_cws_logf(float x) {
+  int e = 0;
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if (u < 0x00800000u) {
+    float y = x * 16777216.0f;
+    memcpy(&u, &y, 4);
+    e = -24;
+  }
+  e += (int)(u >> 23) - 127;
+  uint32_t mu = (u & 0x007FFFFFu) | 0x3F800000u;
+  float m;
+  memcpy(&m, &mu, 4);
+  if (m > 1.41421354f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  float s = (m - 1.0f) / (m + 1.0f);
+  float z = s * s;
+  float p = 0.222222224f;
+  p = p * z + 0.285714298f;
+  p = p * z + 0.400000006f;
+  p = p * z + 0.666666687f;
+  p = p * z + 2.0f;
+  float lnm = p * s;
+  float ef = (float)e;
+  return ef * 0.693145752f + (ef * 1.42860677e-06f + lnm);
+}
+
+/* samples [n][S] of (index, t) int32 pairs */
+void or_cws_sketch(const float* x, int64_t n, int d, int S, const float* tab, int32_t* out) {
+  float* L = (float*)malloc(sizeof(float) * (size_t)d);
+  for (int64_t r = 0; r < n; ++r) {
+    for (int i = 0; i < d; ++i) {
+      float v = x[r * d + i];
+      L[i] = (v > 0.0f && v < INFINITY) ? or_cws_logf(v) : INFINITY;
+    }
+    for (int j = 0; j < S; ++j) {
+      float best = INFINITY;
+      int bk = d, bt = 0;
+      for (int i = 0; i < d; ++i) {
+        if (L[i] == INFINITY) continue;
+        const float* T = tab + ((size_t)i * S + j) * 4;
+        float v = L[i] * T[1] + T[3];
+        v = fminf(fmaxf(v, -1.0e9f), 1.0e9f);
+        float tf = floorf(v);
+        float la = T[2] - T[0] * ((tf - T[3]) + 1.0f);
+        if (la < best) {
+          best = la;
+          bk = i;
+          bt = (int)tf;
+        }
+      }
+      out[(r * S + j) * 2] = bk;
+      out[(r * S + j) * 2 + 1] = bt;
+    }
+  }
+  free(L);
+}
+
+/* ---------------------------------------------------------------------------
  * Sketched scans: top-C by (sketch distance, id), exact re-rank, top-k
  * (sketchedDistanceScanners.cuh, candidateSetScanner.cuh)
- * kind: 3 Hamming words, 4 byte sketches, 5 one-bit words, 6 JL floats
+ * kind: 3 Hamming words, 4 byte sketches, 5 one-bit words, 6 JL floats,
+ * 10 CWS (index, t) pairs (width = samples)
  * ------------------------------------------------------------------------- */
 static float sketch_dist(int kind, const void* xs, const void* qs, int64_t i, int64_t qi, int width) {
+  if (kind == 10) {
+    const int32_t* a = (const int32_t*)xs + i * width * 2;
+    const int32_t* b = (const int32_t*)qs + qi * width * 2;
+    int m = 0;
+    for (int w = 0; w < width; ++w) m += (a[2 * w] == b[2 * w] && a[2 * w + 1] == b[2 * w + 1]) ? 1 : 0;
+    return 1.0f - (float)m / (float)width;
+  }
   if (kind == 6) {
     const float* a = (const float*)xs + i * width;
     const float* b = (const float*)qs + qi * width;
