@@ -146,6 +146,7 @@ def make_data(seed_offset: int):
 
 
 FP64_RECHECK = -1  # lshg_options.fp64_recheck of the benchmarked index
+CWS_PLANES = 16    # bit planes of the benchmarked CWS index's codes (read from the index)
 
 
 def build_index(L, x, path: str):
@@ -201,10 +202,10 @@ def algorithmic(path: str, prof: dict, nq: int, lsh_counts=None):
     # word on the integer ALU pipe; work = Q x N x 64 plane words (256 samples)
     if path == "wmh" and "scan_bytes_filter" in prof:
         return "scan_bytes_filter", "alu", nq * N_BASE * 64 / 1e9, "Gword/s"
-    # CWS codes through the same filter: 16 bit planes a 32-sample group, 128 plane words a
-    # pair at 256 samples
+    # CWS codes through the same filter: 8 planes a 32-sample group for dictionary ranks,
+    # 16 for raw codes (64 or 128 plane words a pair at 256 samples)
     if path == "cws":
-        return "scan_cws", "alu", nq * N_BASE * 128 / 1e9, "Gword/s"
+        return "scan_cws", "alu", nq * N_BASE * 8 * CWS_PLANES / 1e9, "Gword/s"
     # sketch scans on the popcount path are integer-bound at these batch sizes: work = sketch
     # words compared (one XOR + POPC each, zero-byte count for byte samples), Q x N x words
     if path == "simhash":
@@ -454,6 +455,9 @@ def main():
     x, q = make_data(rank)
     tb = time.perf_counter()
     idx = build_index(L, x, args.path)
+    global CWS_PLANES
+    if args.path == "cws":  # bit planes the CWS scan compares (8: dictionary ranks, 16: raw codes)
+        CWS_PLANES = int(np.frombuffer(idx.export(L.EXPORT_CWS_CODES), np.int32)[4]) or 16
     build_s = time.perf_counter() - tb  # host wall time of the index build (synchronous)
     dev = torch.device("cuda", local)
     qd = torch.from_numpy(q).to(dev)

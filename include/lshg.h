@@ -206,9 +206,10 @@ int lshg_index_query_noalloc(lshg_index* idx, const float* d_queries, int N_quer
  *  5 = query counters (uint64 [2], cumulative since the build or load: LSH bucket
  *      entries walked, distinct LSH candidates scored); read after the queries' streams
  *      have been synchronised
- *  6 = consistent-weighted-sampling code plan (int32 [5]: min and max t over the base's
+ *  6 = consistent-weighted-sampling code plan (int32 [6]: min and max t over the base's
  *      samples, code bits of the dimension index and of t, bit planes of the sliced codes
- *      -- 8 or 16, 0 when the codes need more than 16 bits and every scan is direct)
+ *      -- 8 or 16, 0 when the codes need more than 16 bits and every scan is direct --,
+ *      and 1 when the codes are ranks in per-position dictionaries of the base's codes)
  * If dst is NULL only *bytes is set. */
 int lshg_index_export(lshg_index* idx, int what, void* dst, size_t* bytes);
 /* Hash/sketch queries with the index's random vectors: sketches and keys as in export. */

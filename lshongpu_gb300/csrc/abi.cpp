@@ -342,13 +342,14 @@ int lshg_index_export(lshg_index* idx, int what, void* dst, size_t* bytes) {
       case 3: src = I.offsets.ptr; nb = I.offsets.bytes(); break;
       case 4: src = I.buckets.ptr; nb = I.buckets.bytes(); break;
       case 5: src = I.qstats.ptr; nb = I.qstats.bytes(); break;
-      case 6: nb = 5 * sizeof(int32_t); break;
+      case 6: nb = 6 * sizeof(int32_t); break;
       default: throw Error(LSHG_ERR_INVALID_ARGUMENT, "unknown export item");
     }
     *bytes = nb;
     if (!dst || nb == 0) return;
     if (what == 6) {  // CWS code plan (zeros for other sketch kinds)
-      const int32_t plan[5] = {I.cws.tmin, I.cws.tmax, I.cws.kb, I.cws.tb, I.sk_kind == 10 ? I.cws.pl : 0};
+      const int32_t plan[6] = {I.cws.tmin, I.cws.tmax, I.cws.kb, I.cws.tb, I.sk_kind == 10 ? I.cws.pl : 0,
+                               I.cws.dict};
       memcpy(dst, plan, sizeof plan);
       return;
     }

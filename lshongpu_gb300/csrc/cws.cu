@@ -21,8 +21,11 @@
 //
 // Scan: samples are recoded against the base's range of t (a dimension index and an
 // offset of t, at most 16 bits; a query sample outside the range gets a code no base
-// sample has) and bit-sliced into 8 or 16 planes, then go through the byte scan's
-// threshold filter (slice_filter.cuh).  Batches below 64 queries, queries whose
+// sample has).  When no sample position holds more than 255 distinct base codes, each
+// code is replaced by its rank in its position's dictionary (a byte; 255 for a code the
+// base does not have there), so the scan compares bytes like the byte weighted MinHash;
+// otherwise the 16-bit codes are kept.  The codes are bit-sliced into 8 or 16 planes and
+// go through the byte scan's threshold filter (slice_filter.cuh).  Batches below 64 queries, queries whose
 // survivors the filter cannot select exactly, and bases whose codes would need more than
 // 16 bits are scanned directly over the (index, t) pairs.  Either way the candidates are
 // the exact top-C by (1 - matches / S, id).
@@ -128,14 +131,60 @@ __global__ void cws_range_kernel(const int2* __restrict__ smp, int64_t total, in
   }
 }
 
+// Per-position code dictionary of the base: bit `code` of row j of `bits` ([S][2^P / 32]
+// words) is set when some base point's sample j has that code.
+__global__ void cws_dict_mark_kernel(const int2* __restrict__ smp, int64_t total, int S, int tmin, int tb, int words,
+                                     uint32_t* __restrict__ bits) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % S);
+    const int2 v = smp[i];
+    const uint32_t code = ((uint32_t)v.x << tb) | (uint32_t)(v.y - tmin);  // base samples: always in range
+    atomicOr(&bits[(int64_t)j * words + (code >> 5)], 1u << (code & 31));
+  }
+}
+
+// One block a sample position: rank of every code among the position's set bits (255 for
+// codes not set, and for ranks past 254 -- the host then drops the dictionary), and the
+// position's code count into *maxcount.
+__global__ void __launch_bounds__(256) cws_dict_rank_kernel(const uint32_t* __restrict__ bits, int words,
+                                                            uint8_t* __restrict__ rank, int* __restrict__ maxcount) {
+  __shared__ int part[256];
+  const int j = blockIdx.x, tid = threadIdx.x;
+  const uint32_t* b = bits + (int64_t)j * words;
+  const int per = (words + 255) / 256, w0 = tid * per, w1 = min(words, w0 + per);
+  int own = 0;
+  for (int w = w0; w < w1; ++w) own += __popc(b[w]);
+  part[tid] = own;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {  // inclusive scan
+    const int v = tid >= o ? part[tid - o] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int base = part[tid] - own;
+  uint8_t* r = rank + ((int64_t)j * words << 5);
+  for (int w = w0; w < w1; ++w) {
+    const uint32_t x = b[w];
+    for (int k = 0; k < 32; ++k) {
+      const int at = base + __popc(x & ((1u << k) - 1u));
+      r[w * 32 + k] = ((x >> k) & 1u) && at < 255 ? (uint8_t)at : (uint8_t)255;
+    }
+    base += __popc(x);
+  }
+  if (tid == 255) atomicMax(maxcount, part[255]);
+}
+
 // Samples [rows][S] -> codes bit-sliced into rows of ng * PL words (word g PL + b holds
 // bit b of the codes of samples 32 g .. 32 g + 31).  code = (i << tb) | (t - tmin) for
 // i <= d and t in [tmin, tmin + 2^tb); anything else gets the code (d + 1) << tb, which no
 // base sample has.  Samples past S get `pad` (0 for the base, all ones for queries, so
 // padding never matches).  One thread a (row, group).
+// rank (optional, dictionary codes): [S][2^rlog] bytes, the code's rank among the codes the
+// base has at that sample position, 255 for a code no base sample has there.
 template <int PL>
 __global__ void cws_slice_kernel(const int2* __restrict__ smp, int64_t rows, int S, int ng, int d, int tmin, int tb,
-                                 uint32_t pad, uint32_t* __restrict__ out) {
+                                 const uint8_t* __restrict__ rank, int rlog, uint32_t pad, uint32_t* __restrict__ out) {
   const int64_t total = rows * ng;
   const uint32_t tspan = 1u << tb, sentinel = (uint32_t)(d + 1) << tb;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
@@ -151,6 +200,7 @@ __global__ void cws_slice_kernel(const int2* __restrict__ smp, int64_t rows, int
         const int64_t dt = (int64_t)v.y - tmin;
         c = (v.x >= 0 && v.x <= d && dt >= 0 && dt < (int64_t)tspan) ? (((uint32_t)v.x << tb) | (uint32_t)dt)
                                                                       : sentinel;
+        if (rank) c = rank[((int64_t)j << rlog) + c];
       }
       code[s] = c;
     }
@@ -357,6 +407,38 @@ CwsCodes cws_plan_codes(const uint32_t* xs, int64_t n, int S, int d, cudaStream_
   return c;
 }
 
+bool cws_build_dict(const uint32_t* xs, int64_t n, int S, CwsCodes& c, DevBuf<uint8_t>& rank, cudaStream_t s) {
+  const int P = c.kb + c.tb;
+  if (c.pl != 16 || n <= 0) return false;  // codes of at most 8 bits need no dictionary
+  const int rlog = std::max(P, 5), words = 1 << (rlog - 5);
+  DevBuf<uint32_t> bits((size_t)S * words, s);
+  LSHG_CUDA(cudaMemsetAsync(bits.ptr, 0, bits.bytes(), s));
+  const int64_t total = n * S;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
+  cws_dict_mark_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const int2*>(xs), total, S, c.tmin, c.tb, words,
+                                              bits.ptr);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+  rank.alloc((size_t)S << rlog, s);
+  DevBuf<int> maxc(1, s);
+  LSHG_CUDA(cudaMemsetAsync(maxc.ptr, 0, sizeof(int), s));
+  cws_dict_rank_kernel<<<S, 256, 0, s>>>(bits.ptr, words, rank.ptr, maxc.ptr);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
+  int h = 0;
+  LSHG_CUDA(cudaMemcpyAsync(&h, maxc.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LSHG_CUDA(cudaStreamSynchronize(s));
+  if (h > 255) {  // some position holds more than 255 codes: keep the 16-plane codes
+    rank.release();
+    return false;
+  }
+  c.dict = 1;
+  c.pl = 8;
+  c.rlog = rlog;
+  c.rank = rank.ptr;
+  return true;
+}
+
 void launch_cws_slice(const uint32_t* smp, int64_t rows, int S, int d, const CwsCodes& c, bool query, uint32_t* out,
                       cudaStream_t s) {
   const int ng = (S + 31) / 32;
@@ -365,9 +447,11 @@ void launch_cws_slice(const uint32_t* smp, int64_t rows, int S, int d, const Cws
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
   const int2* v = reinterpret_cast<const int2*>(smp);
   if (c.pl == 8)
-    cws_slice_kernel<8><<<blocks, 256, 0, s>>>(v, rows, S, ng, d, c.tmin, c.tb, query ? 0xFFu : 0u, out);
+    cws_slice_kernel<8><<<blocks, 256, 0, s>>>(v, rows, S, ng, d, c.tmin, c.tb, c.rank, c.rlog, query ? 0xFFu : 0u,
+                                               out);
   else
-    cws_slice_kernel<16><<<blocks, 256, 0, s>>>(v, rows, S, ng, d, c.tmin, c.tb, query ? 0xFFFFu : 0u, out);
+    cws_slice_kernel<16><<<blocks, 256, 0, s>>>(v, rows, S, ng, d, c.tmin, c.tb, nullptr, 0, query ? 0xFFFFu : 0u,
+                                                out);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }

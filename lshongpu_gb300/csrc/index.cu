@@ -43,6 +43,7 @@ void tile_sketches(Index& I, cudaStream_t s) {
   if (I.sk_kind == 10) {  // CWS: codes against the base's range of t, bit-sliced for the filter scan
     I.cws = cws_plan_codes(I.xs.ptr, I.n, I.cws_S, I.d, s);
     if (I.cws.pl && I.p.opt.sketch_scan != 1) {
+      cws_build_dict(I.xs.ptr, I.n, I.cws_S, I.cws, I.cws_rank, s);
       const int wsl = I.cws_S / 32 * I.cws.pl;
       DevBuf<uint32_t> sl((size_t)I.n * wsl, s);
       launch_cws_slice(I.xs.ptr, I.n, I.cws_S, I.d, I.cws, false, sl.ptr, s);
@@ -316,7 +317,7 @@ Index::~Index() {
   sk_planes.release(); sk_split.release(); sk_pnorm.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
   xbf.release(); xbf_scale.release(); xf8.release(); xnorm64.release(); xst.release(); qstats.release();
-  cws_tab.release();
+  cws_tab.release(); cws_rank.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();

@@ -69,6 +69,7 @@ struct Index {
   int cws_S = 0;             // CWS samples a vector; xs rows are S (index, t) int32 pairs
   DevBuf<float> cws_tab;     // CWS draw table [d][S][4]
   CwsCodes cws;              // CWS code plan (derived from xs at build and at load)
+  DevBuf<uint8_t> cws_rank;  // CWS per-position code dictionaries (derived, not stored)
 
   // LSH
   int key_kind = 0;

@@ -109,6 +109,9 @@ struct CwsCodes {
   int tmin = 0, tmax = 0;  // range of t over the base's samples
   int kb = 0, tb = 0;      // code bits of the dimension index and of t - tmin
   int pl = 0;              // bit planes of the sliced codes (8 or 16); 0: codes need more than 16 bits
+  int dict = 0;            // 1: codes are ranks in per-position dictionaries of the base's codes
+  int rlog = 0;            // dictionary rows of 2^rlog bytes
+  const uint8_t* rank = nullptr;  // dictionaries [S][2^rlog] (device; owned by the index)
 };
 // Draw table [d][S] of (r, 1/r, ln c, beta) as 4 floats.
 void cws_tables(int d, int S, std::vector<float>& tab);
@@ -116,6 +119,9 @@ void cws_tables(int d, int S, std::vector<float>& tab);
 void launch_cws_sketch(const float* x, int64_t rows, int d, int S, const float* tab, uint32_t* out, cudaStream_t s);
 // Code plan from the base's samples (synchronises the stream to read their range of t).
 CwsCodes cws_plan_codes(const uint32_t* xs, int64_t n, int S, int d, cudaStream_t s);
+// Per-position dictionaries of the base's 9..16-bit codes: on success (every position
+// holds at most 255 codes) `rank` holds them and c switches to 8-plane dictionary codes.
+bool cws_build_dict(const uint32_t* xs, int64_t n, int S, CwsCodes& c, DevBuf<uint8_t>& rank, cudaStream_t s);
 // Samples -> codes bit-sliced into rows of (S / 32) * pl words (queries: padding never matches).
 void launch_cws_slice(const uint32_t* smp, int64_t rows, int S, int d, const CwsCodes& c, bool query, uint32_t* out,
                       cudaStream_t s);

@@ -5,7 +5,8 @@ the index's (index, t) pairs -- base and queries -- are compared bit for bit wit
 oracle's restatement; the scan must select exactly the oracle's top-C by
 (1 - matches / S, id), so after the generalized-Jaccard re-rank ids and distances are
 compared exactly.  Cases cover the three scan forms: the threshold filter over 16-plane
-and 8-plane codes (batches of 64 queries and more), the direct scan over the pairs
+codes, 8-plane codes and per-position dictionary ranks (batches of 64 queries and
+more), the direct scan over the pairs
 (small batches, listed queries, and bases whose codes need more than 16 bits), and ties
 that overflow the filter's candidate arrays.
 """
@@ -58,7 +59,21 @@ def test_cws_matches_oracle(engine, orc, C, n, S, nq):
     q = datasets.sparse_gamma(nq, 100, 42)
     idx = build(engine, x, S, C)
     plan = check_against_oracle(engine, orc, idx, x, q, S, C)
-    assert plan[4] == 16  # d = 100: 7 index bits and t offsets above 1 bit
+    # d = 100: 7 index bits and a few bits of t, at most ~150 distinct codes a position --
+    # dictionary ranks, compared as bytes
+    assert plan[4] == 8 and plan[5] == 1
+
+
+def test_cws_sixteen_plane_codes(engine, orc):
+    """Log-normal weights over 500 dimensions: 15-bit codes with more than 255 distinct
+    codes at some position, so the 16-bit codes are sliced into 16 planes."""
+    rng = np.random.default_rng(5)
+    d = 500
+    x = (np.exp(rng.normal(0, 1.5, (40000, d))) * (rng.random((40000, d)) < 0.5)).astype(np.float32)
+    q = (np.exp(rng.normal(0, 1.5, (80, d))) * (rng.random((80, d)) < 0.5)).astype(np.float32)
+    idx = build(engine, x, 64, 256)
+    plan = check_against_oracle(engine, orc, idx, x, q, 64, 256)
+    assert plan[4] == 16 and plan[5] == 0
 
 
 def test_cws_eight_plane_codes(engine, orc):
@@ -68,7 +83,7 @@ def test_cws_eight_plane_codes(engine, orc):
     q = (0.5 + 0.5 * rng.random((80, 3))).astype(np.float32)
     idx = build(engine, x, 64, 256)
     plan = check_against_oracle(engine, orc, idx, x, q, 64, 256)
-    assert plan[4] == 8
+    assert plan[4] == 8 and plan[5] == 0
 
 
 def test_cws_wide_codes_scan_directly(engine, orc):
