@@ -394,6 +394,67 @@ __global__ void rerank_select_kernel(const uint64_t* __restrict__ keys_in, int C
   }
 }
 
+// The same select when only the first 128 places matter (k <= 128: the output and the
+// FP64 re-check, which never looks past place 128): each of the 16 warps sorts its 32 E
+// keys in registers and keeps the first 128, and four rounds of "min against the reversed
+// partner list, then one bitonic merge" fold the 16 lists into the 128 smallest, sorted --
+// the same 128 keys in the same order as sorting all C, without a block-wide sort.
+template <int DIST, int E>
+__global__ void __launch_bounds__(512) rerank_top_kernel(const uint64_t* __restrict__ keys_in, int C,
+                                                         const float* __restrict__ x, int d,
+                                                         const float* __restrict__ q, int k,
+                                                         lshg_point* __restrict__ out, float band_abs, float band_rel,
+                                                         const double* __restrict__ xn64,
+                                                         const RerankBounds* __restrict__ kx) {
+  constexpr int P = 128, EP = P / 32;
+  __shared__ uint64_t lists[16][P];
+  extern __shared__ __align__(16) unsigned char rsm[];
+  float* qr = reinterpret_cast<float*>(rsm);
+  const int qi = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) qr[j] = q[(int64_t)qi * d + j];
+  const uint64_t* src = keys_in + (int64_t)qi * C + warp * (32 * E);
+  uint64_t v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = src[e * 32 + lane];
+  warp_bitonic<E>(v, lane, false);
+#pragma unroll
+  for (int e = 0; e < EP; ++e) lists[warp][e * 32 + lane] = e < E ? v[e] : kEmptyKey;
+  __syncthreads();
+#pragma unroll
+  for (int half = 8; half >= 1; half >>= 1) {
+    if (warp < half) {
+      // a ascending, b ascending: min(a[i], b[P - 1 - i]) is bitonic and holds the P smallest
+      uint64_t a[EP];
+#pragma unroll
+      for (int e = 0; e < EP; ++e) {
+        const uint64_t av = lists[warp][e * 32 + lane];
+        const uint64_t bv = lists[warp + half][(EP - 1 - e) * 32 + (31 - lane)];
+        a[e] = av < bv ? av : bv;
+      }
+      warp_bitonic<EP>(a, lane, true);
+#pragma unroll
+      for (int e = 0; e < EP; ++e) lists[warp][e * 32 + lane] = a[e];
+    }
+    __syncthreads();
+  }
+  uint64_t* keys = lists[0];
+  if (band_abs >= 0.0f) {
+    fp64_boundary<DIST>(keys, P, k, x, xn64, d, qr, band_abs, band_rel);
+    const int nx = kx ? imin(kx->n, 4) : 0;
+    for (int b = 0; b < nx; ++b) {
+      const int kb = kx->k[b];
+      if (kb >= 1 && kb < k) fp64_boundary<DIST>(keys, P, kb, x, xn64, d, qr, band_abs, band_rel);
+    }
+  }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    const uint64_t kk = keys[i];
+    lshg_point pt;
+    if (kk == kEmptyKey) { pt.ID = -1; pt.distance = kEmptyDistance; }
+    else { pt.ID = key_id(kk); pt.distance = key_dist(kk); }
+    out[(int64_t)qi * k + i] = pt;
+  }
+}
+
 __global__ void keys_to_points_kernel(const uint64_t* __restrict__ keys, int nq, int C, int k,
                                       lshg_point* __restrict__ out) {
   int64_t total = (int64_t)nq * k;
@@ -464,10 +525,21 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
                                                                          gk.ptr, err);                          \
     count_launch();                                                                                             \
     LSHG_CHECK_LAUNCH();                                                                                        \
-    LSHG_CUDA(cudaFuncSetAttribute(rerank_select_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
-                                   (int)select_smem));                                                          \
-    rerank_select_kernel<DV><<<nq, 512, select_smem, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel, xn64, \
-                                                          kb);                                                \
+    if (k <= 128 && C == 4096)                                                                                  \
+      rerank_top_kernel<DV, 8><<<nq, 512, (size_t)d * 4, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel,   \
+                                                              xn64, kb);                                        \
+    else if (k <= 128 && C == 2048)                                                                             \
+      rerank_top_kernel<DV, 4><<<nq, 512, (size_t)d * 4, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel,   \
+                                                              xn64, kb);                                        \
+    else if (k <= 128 && C == 1024)                                                                             \
+      rerank_top_kernel<DV, 2><<<nq, 512, (size_t)d * 4, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel,   \
+                                                              xn64, kb);                                        \
+    else {                                                                                                      \
+      LSHG_CUDA(cudaFuncSetAttribute(rerank_select_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                                     (int)select_smem));                                                        \
+      rerank_select_kernel<DV><<<nq, 512, select_smem, s>>>(gk.ptr, C, x, d, q, k, out, band_abs, band_rel,     \
+                                                            xn64, kb);                                          \
+    }                                                                                                           \
   } while (0)
     switch (dist) {
       case DIST_ANGULAR: LSHG_RR2(DIST_ANGULAR); break;

@@ -656,7 +656,10 @@ void launch_filter_scan(const CUtensorMap& ma, const CUtensorMap& mb, const CUte
 
 void launch_tau_select(const float* gmax, int nq, int M, int rank, float margin, float* tau, cudaStream_t s) {
   ProfScope _ps("tc_tau_select", s);
-  if (M <= 32 * kTauRegs && M % 4 == 0)
+  // the register slots a lane walks in every bisection step: as few as cover M
+  if (M <= 32 * (kTauRegs / 2) && M % 4 == 0)
+    tau_select_reg_kernel<kTauRegs / 2><<<ceil_div(nq, 8), 256, 0, s>>>(gmax, nq, M, rank, margin, tau);
+  else if (M <= 32 * kTauRegs && M % 4 == 0)
     tau_select_reg_kernel<kTauRegs><<<ceil_div(nq, 8), 256, 0, s>>>(gmax, nq, M, rank, margin, tau);
   else
     tau_select_kernel<<<ceil_div(nq, 8), 256, 0, s>>>(gmax, nq, M, rank, margin, tau);
