@@ -72,7 +72,8 @@ int batch_class(const Index& I, int k) {
   if (I.p.framework == 0 && impl == 9) return 0;  // 128 candidates at every k
   int kp = 32;
   while (kp < k) kp <<= 1;
-  const bool sketched = I.p.framework == 0 ? (impl >= 3 && impl <= 6) : (I.p.runWithSketchedData && I.sk_kind);
+  const bool sketched =
+      I.p.framework == 0 ? ((impl >= 3 && impl <= 6) || impl == 10) : (I.p.runWithSketchedData && I.sk_kind);
   if (sketched) return std::max(I.C, kp);
   return 0;
 }

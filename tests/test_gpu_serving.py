@@ -175,3 +175,26 @@ def test_load_rejects_inconsistent_files(engine):
         with open(p, "wb") as f:
             f.write(good)
         assert np.array_equal(engine.Index.load(p).query(q, 32), ix.query(q, 32))
+
+
+def test_cws_index_same_alone_and_in_the_mix(engine):
+    """A consistent-weighted-sampling index (64 candidates, so k = 100 needs 128) behind the
+    serving loop: requests of every k are coalesced only where the candidate count is the
+    same, and each result equals the request alone."""
+    x = datasets.sparse_gamma(20000, D, 71)
+    cws = engine.Index(x, implementation=engine.IMPL_CWS, distanceFunc=2, sketchDim=64,
+                       options=engine.make_options(candidates=64))
+    rng = np.random.default_rng(11)
+    srv = engine.Server(max_batch=1024, streams=2, use_graphs=True, batch_window_us=20_000)
+    srv.add_index(0, cws)
+    reqs = []
+    for t in range(30):
+        nq = int(np.exp(rng.uniform(0, np.log(200))))
+        k = int(rng.choice([10, 32, 100]))
+        q = datasets.sparse_gamma(nq, D, 3000 + t)
+        reqs.append((q, k, srv.submit(0, q, k)))
+    for q, k, tk in reqs:
+        out, _ = srv.wait(tk)
+        assert np.array_equal(out, cws.query(q, k))
+    assert srv.stats()["completed"] == len(reqs)
+    srv.close()
