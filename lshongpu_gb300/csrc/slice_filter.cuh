@@ -13,10 +13,9 @@
 // MODE 1: keep every point with at least tau[q] matches (keys make_key(-matches, id)).
 // A position p covers tile p * tstride.
 //
-// One CTA of 16 warps an SM serves 64 queries at a time.  Work is the flat sequence of
-// (query block, position) items, query block major; each CTA takes an equal contiguous
-// range, so it changes query block at most a few times and no CTA gets more than one
-// tile above the average.  Tiles are staged in shared memory by 1-D bulk copies, STAGES
+// One CTA of 16 warps an SM serves 64 queries at a time.  Each CTA walks its own sequence
+// of (query block, position) items (make_walk / locate below), within one chunk or one
+// tile of every other CTA's length.  Tiles are staged in shared memory by 1-D bulk copies, STAGES
 // ahead; the last warp to finish a tile issues the copy that refills its buffer, so warps
 // never wait on one another between tiles.  A thread owns two points of a tile (p and
 // p + 64) and 8 of the 64 queries: each query word it loads from shared memory (the same
@@ -66,6 +65,64 @@ struct Layout {
   static_assert(SMEM <= kSmemMax, "shared memory per CTA");
 };
 
+// MODE 1 walks the base in chunks of kChunk positions.  A unit is (chunk, query block),
+// numbered chunk-major, and CTA b takes units b, b + G, b + 2G, ...: the G CTAs then work
+// on the same chunk at a time, so a base tile comes from DRAM about once a batch and from
+// L2 for the other query blocks (a CTA walking one query block through the whole base,
+// about as large as L2, had read it from DRAM about once a query block).  MODE 0 samples
+// a small part of the base and gives each CTA an equal contiguous range of
+// (query block, position) items, query block major (one histogram flush a block).
+constexpr int kChunk = 64;
+
+// This CTA's items, local index li in [0, len).
+struct Walk {
+  int64_t beg = 0, len = 0;  // MODE 0: global items [beg, beg + len)
+  int nf = 0, wl = 0;        // MODE 1: units in full chunks, width of the last chunk
+};
+
+template <int MODE>
+__device__ __forceinline__ Walk make_walk(int NP, int QB) {
+  Walk w;
+  const int G = gridDim.x, b = blockIdx.x;
+  if (MODE == 0) {
+    const int64_t total = (int64_t)QB * NP;
+    w.beg = total * b / G;
+    w.len = total * (b + 1) / G - w.beg;
+    return w;
+  }
+  const int nch = (NP + kChunk - 1) / kChunk;
+  w.wl = NP - (nch - 1) * kChunk;
+  const int64_t U = (int64_t)nch * QB, Uf = (int64_t)(nch - 1) * QB;
+  const int64_t mine = U > b ? (U - b + G - 1) / G : 0;
+  w.nf = (int)(Uf > b ? (Uf - b + G - 1) / G : 0);
+  w.len = (int64_t)w.nf * kChunk + (mine - w.nf) * w.wl;
+  return w;
+}
+
+// (query block, position) of local item li.
+template <int MODE>
+__device__ __forceinline__ void locate(const Walk& w, int64_t li, int NP, int QB, int& qb, int& pos) {
+  if (MODE == 0) {
+    const int64_t it = w.beg + li;
+    qb = (int)(it / NP);
+    pos = (int)(it - (int64_t)qb * NP);
+    return;
+  }
+  int64_t k, j;
+  if (li < (int64_t)w.nf * kChunk) {
+    k = li / kChunk;
+    j = li - k * kChunk;
+  } else {
+    const int64_t l2 = li - (int64_t)w.nf * kChunk;
+    k = w.nf + l2 / w.wl;
+    j = l2 - (k - w.nf) * w.wl;
+  }
+  const int64_t u = blockIdx.x + k * gridDim.x;
+  const int c = (int)(u / QB);
+  qb = (int)(u - (int64_t)c * QB);
+  pos = c * kChunk + (int)j;
+}
+
 template <int MODE, int NG, int PL>
 __global__ void __launch_bounds__(kBThreads, 1)
     sliced_filter_kernel(const uint4* __restrict__ xst, int64_t n, const uint32_t* __restrict__ qsl, int nq, int NP,
@@ -87,11 +144,13 @@ __global__ void __launch_bounds__(kBThreads, 1)
   const int tid = threadIdx.x, lane = tid & 31, pl = tid & 63, qo = (tid >> 6) * kQT;
   const unsigned lt = (1u << lane) - 1u;
 
-  const int64_t total = (int64_t)((nq + kBQ - 1) / kBQ) * NP;
-  const int64_t beg = total * blockIdx.x / gridDim.x, end = total * (blockIdx.x + 1) / gridDim.x;
+  const int QB = (nq + kBQ - 1) / kBQ;
+  const Walk wk = make_walk<MODE>(NP, QB);
+  const int64_t beg = 0, end = wk.len;  // local item indices
   // item `it` -> its tile copied into stage (it - beg) % ST
   auto issue = [&](int64_t it) {
-    const int qb = (int)(it / NP), pos = (int)(it - (int64_t)qb * NP);
+    int qb, pos;
+    locate<MODE>(wk, it, NP, QB, qb, pos);
     const int st = (int)((it - beg) % ST);
     const uint32_t bar = bar0 + 8 * st;
     slast[st] = it;
@@ -113,7 +172,8 @@ __global__ void __launch_bounds__(kBThreads, 1)
   bool live = true;  // false once a wait gave up: the rest of the range is walked without work
   int cur = -1;
   for (int64_t it = beg; it < end; ++it) {
-    const int qb = (int)(it / NP), pos = (int)(it - (int64_t)qb * NP);
+    int qb, pos;
+    locate<MODE>(wk, it, NP, QB, qb, pos);
     const int q0 = qb * kBQ;
     if (qb != cur) {  // all warps meet here: reload the block's queries
       __syncthreads();
@@ -270,7 +330,8 @@ void run_ng(const uint4* xst, int64_t n, const uint32_t* qsl, int nq, int NP, in
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   int per_sm = 0;
   LSHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBThreads, smem));
-  const int64_t total = (int64_t)ceil_div(nq, kBQ) * NP;
+  const int64_t total = MODE == 0 ? (int64_t)ceil_div(nq, kBQ) * NP           // items
+                                  : (int64_t)ceil_div(nq, kBQ) * ceil_div(NP, kChunk);  // units
   const int grid = (int)std::min<int64_t>(total, (int64_t)num_sms() * std::max(1, per_sm));
   kern<<<grid, kBThreads, smem, s>>>(xst, n, qsl, nq, NP, tstride, tau, hist, bins, cnt, cand, cap, err);
   count_launch();
