@@ -40,6 +40,7 @@ constexpr int kQT = 8;         // queries a thread
 constexpr int kBThreads = 512;
 constexpr int kBWarps = kBThreads / 32;
 constexpr int kSmemMax = 232448;  // shared memory a CTA may use
+constexpr int64_t kL2Half = 64ll << 20;  // bases above this are walked chunk-major
 
 template <int MODE, int NG, int PL>
 struct Layout {
@@ -65,68 +66,105 @@ struct Layout {
   static_assert(SMEM <= kSmemMax, "shared memory per CTA");
 };
 
-// MODE 1 walks the base in chunks of kChunk positions.  A unit is (chunk, query block),
+// A base larger than half the L2 is walked in chunks of `chunk` positions (8..64: at least
+// ~24 units a CTA, so that the last units leave little imbalance).  A unit is (chunk, query
+// block),
 // numbered chunk-major, and CTA b takes units b, b + G, b + 2G, ...: the G CTAs then work
 // on the same chunk at a time, so a base tile comes from DRAM about once a batch and from
 // L2 for the other query blocks (a CTA walking one query block through the whole base,
-// about as large as L2, had read it from DRAM about once a query block).  MODE 0 samples
-// a small part of the base and gives each CTA an equal contiguous range of
-// (query block, position) items, query block major (one histogram flush a block).
-constexpr int kChunk = 64;
-
+// about as large as L2, had read it from DRAM about once a query block).  Otherwise
+// (chunk = 0: the prepass, which samples a small part of the base, and bases that stay in
+// L2) each CTA takes an equal contiguous range of (query block, position) items, query
+// block major: fewer query-block switches (and histogram flushes).
 // This CTA's items, local index li in [0, len).
 struct Walk {
   int64_t beg = 0, len = 0;  // MODE 0: global items [beg, beg + len)
   int nf = 0, wl = 0;        // MODE 1: units in full chunks, width of the last chunk
 };
 
-template <int MODE>
-__device__ __forceinline__ Walk make_walk(int NP, int QB) {
+__device__ __forceinline__ Walk make_walk(int NP, int QB, int chunk) {
   Walk w;
   const int G = gridDim.x, b = blockIdx.x;
-  if (MODE == 0) {
+  if (chunk == 0) {
     const int64_t total = (int64_t)QB * NP;
     w.beg = total * b / G;
     w.len = total * (b + 1) / G - w.beg;
     return w;
   }
-  const int nch = (NP + kChunk - 1) / kChunk;
-  w.wl = NP - (nch - 1) * kChunk;
+  const int nch = (NP + chunk - 1) / chunk;
+  w.wl = NP - (nch - 1) * chunk;
   const int64_t U = (int64_t)nch * QB, Uf = (int64_t)(nch - 1) * QB;
   const int64_t mine = U > b ? (U - b + G - 1) / G : 0;
   w.nf = (int)(Uf > b ? (Uf - b + G - 1) / G : 0);
-  w.len = (int64_t)w.nf * kChunk + (mine - w.nf) * w.wl;
+  w.len = (int64_t)w.nf * chunk + (mine - w.nf) * w.wl;
   return w;
 }
 
 // (query block, position) of local item li.
-template <int MODE>
-__device__ __forceinline__ void locate(const Walk& w, int64_t li, int NP, int QB, int& qb, int& pos) {
-  if (MODE == 0) {
+__device__ __forceinline__ void locate(const Walk& w, int64_t li, int NP, int QB, int chunk, int& qb, int& pos) {
+  if (chunk == 0) {
     const int64_t it = w.beg + li;
     qb = (int)(it / NP);
     pos = (int)(it - (int64_t)qb * NP);
     return;
   }
   int64_t k, j;
-  if (li < (int64_t)w.nf * kChunk) {
-    k = li / kChunk;
-    j = li - k * kChunk;
+  if (li < (int64_t)w.nf * chunk) {
+    k = li / chunk;
+    j = li - k * chunk;
   } else {
-    const int64_t l2 = li - (int64_t)w.nf * kChunk;
+    const int64_t l2 = li - (int64_t)w.nf * chunk;
     k = w.nf + l2 / w.wl;
     j = l2 - (k - w.nf) * w.wl;
   }
   const int64_t u = blockIdx.x + k * gridDim.x;
   const int c = (int)(u / QB);
   qb = (int)(u - (int64_t)c * QB);
-  pos = c * kChunk + (int)j;
+  pos = c * chunk + (int)j;
 }
+
+// The same sequence stepped one item at a time (no division but one a unit), for the
+// per-item loop every thread runs; locate() serves the copies issued ahead.
+struct Cursor {
+  int qb = 0, pos = 0;
+  int j = 0, width = 0;  // chunk walk: position within the unit, the unit's width
+  int64_t u = 0;         // chunk walk: unit number
+  __device__ __forceinline__ void unit(int NP, int QB, int chunk) {
+    const int c = (int)(u / QB);
+    qb = (int)(u - (int64_t)c * QB);
+    width = min(chunk, NP - c * chunk);
+    pos = c * chunk;
+    j = 0;
+  }
+  __device__ __forceinline__ void start(const Walk& w, int NP, int QB, int chunk) {
+    if (chunk == 0) {
+      qb = (int)(w.beg / NP);
+      pos = (int)(w.beg - (int64_t)qb * NP);
+      return;
+    }
+    u = blockIdx.x;
+    unit(NP, QB, chunk);
+  }
+  __device__ __forceinline__ void next(int NP, int QB, int chunk) {
+    if (chunk == 0) {
+      if (++pos == NP) {
+        pos = 0;
+        ++qb;
+      }
+      return;
+    }
+    ++pos;
+    if (++j == width) {
+      u += gridDim.x;
+      unit(NP, QB, chunk);
+    }
+  }
+};
 
 template <int MODE, int NG, int PL>
 __global__ void __launch_bounds__(kBThreads, 1)
     sliced_filter_kernel(const uint4* __restrict__ xst, int64_t n, const uint32_t* __restrict__ qsl, int nq, int NP,
-                         int tstride, const int* __restrict__ tau, int* __restrict__ hist, int bins,
+                         int tstride, int chunk, const int* __restrict__ tau, int* __restrict__ hist, int bins,
                          int* __restrict__ cnt, uint64_t* __restrict__ cand, int cap, int* __restrict__ err) {
   using LY = Layout<MODE, NG, PL>;
   constexpr int W = LY::W, NCH = W / 4, ST = LY::STAGES;
@@ -145,12 +183,12 @@ __global__ void __launch_bounds__(kBThreads, 1)
   const unsigned lt = (1u << lane) - 1u;
 
   const int QB = (nq + kBQ - 1) / kBQ;
-  const Walk wk = make_walk<MODE>(NP, QB);
+  const Walk wk = make_walk(NP, QB, chunk);
   const int64_t beg = 0, end = wk.len;  // local item indices
   // item `it` -> its tile copied into stage (it - beg) % ST
   auto issue = [&](int64_t it) {
     int qb, pos;
-    locate<MODE>(wk, it, NP, QB, qb, pos);
+    locate(wk, it, NP, QB, chunk, qb, pos);
     const int st = (int)((it - beg) % ST);
     const uint32_t bar = bar0 + 8 * st;
     slast[st] = it;
@@ -171,9 +209,10 @@ __global__ void __launch_bounds__(kBThreads, 1)
 
   bool live = true;  // false once a wait gave up: the rest of the range is walked without work
   int cur = -1;
-  for (int64_t it = beg; it < end; ++it) {
-    int qb, pos;
-    locate<MODE>(wk, it, NP, QB, qb, pos);
+  Cursor cs;
+  cs.start(wk, NP, QB, chunk);
+  for (int64_t it = beg; it < end; ++it, cs.next(NP, QB, chunk)) {
+    const int qb = cs.qb, pos = cs.pos;
     const int q0 = qb * kBQ;
     if (qb != cur) {  // all warps meet here: reload the block's queries
       __syncthreads();
@@ -330,10 +369,13 @@ void run_ng(const uint4* xst, int64_t n, const uint32_t* qsl, int nq, int NP, in
   LSHG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   int per_sm = 0;
   LSHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBThreads, smem));
-  const int64_t total = MODE == 0 ? (int64_t)ceil_div(nq, kBQ) * NP           // items
-                                  : (int64_t)ceil_div(nq, kBQ) * ceil_div(NP, kChunk);  // units
-  const int grid = (int)std::min<int64_t>(total, (int64_t)num_sms() * std::max(1, per_sm));
-  kern<<<grid, kBThreads, smem, s>>>(xst, n, qsl, nq, NP, tstride, tau, hist, bins, cnt, cand, cap, err);
+  const int64_t slots = (int64_t)num_sms() * std::max(1, per_sm);
+  const int64_t items = (int64_t)ceil_div(nq, kBQ) * NP;
+  const bool big = MODE == 1 && (int64_t)NP * Layout<MODE, NG, PL>::TB > kL2Half;
+  const int chunk = big ? (int)std::max<int64_t>(8, std::min<int64_t>(64, items / (slots * 24))) : 0;
+  const int64_t total = chunk ? (int64_t)ceil_div(nq, kBQ) * ceil_div(NP, chunk) : items;  // units or items
+  const int grid = (int)std::min<int64_t>(total, slots);
+  kern<<<grid, kBThreads, smem, s>>>(xst, n, qsl, nq, NP, tstride, chunk, tau, hist, bins, cnt, cand, cap, err);
   count_launch();
   LSHG_CHECK_LAUNCH();
 }
