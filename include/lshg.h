@@ -31,7 +31,10 @@
  *                                a multiple of 32 up to 256, linear scan only, the
  *                                weighted MinHash preprocessing and generalized-Jaccard
  *                                re-rank
- *   keysImplementation:  3 = SimHash, 4 = WMH byte, 5 = one-bit WMH, 7 = cross-polytope
+ *   keysImplementation:  3 = SimHash, 4 = WMH byte, 5 = one-bit WMH, 7 = cross-polytope,
+ *                        10 = consistent weighted sampling (no reference counterpart:
+ *                            lshg_options.cp_hashes samples a table hashed into
+ *                            bucketKeyBits <= 16 bits, the weighted MinHash preprocessing)
  *   distanceFunc:        1 = angular, 2 = generalized Jaccard, 3 = Euclidean
  */
 #ifndef LSHG_H_
@@ -84,7 +87,8 @@ typedef struct lshg_options_s {
   int thread_queue_size; /* THREAD_QUEUE_SIZE (constants.cuh:6), default 128; the re-rank
                             candidate set is 32 * thread_queue_size (candidateSetScanner.cuh) */
   int candidates;        /* > 0 overrides 32 * thread_queue_size (rounded up to a power of 2) */
-  int cp_hashes;         /* cross-polytope hashes concatenated per table key (reference: 1) */
+  int cp_hashes;         /* cross-polytope hashes concatenated per table key (reference: 1);
+                            CWS keys (keysImplementation 10): samples hashed per table key */
   int cp_rounds;         /* cross-polytope rotation rounds (reference: 3, crossPolyTope.cuh:44) */
   void* stream;          /* cudaStream_t to run on, NULL = a library-owned stream */
   int fp64_recheck;      /* re-score, in double precision on the GPU, the re-ranked candidates

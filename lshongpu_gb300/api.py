@@ -36,6 +36,7 @@ KEYS_SIMHASH = 3
 KEYS_WMH = 4
 KEYS_WMH_ONEBIT = 5
 KEYS_CROSSPOLY = 7
+KEYS_CWS = 10  # consistent weighted sampling (no reference counterpart)
 # sketch_scan option: how Hamming / one-bit Jaccard sketch scans run
 SKETCH_SCAN_AUTO, SKETCH_SCAN_POPCOUNT, SKETCH_SCAN_TENSOR = 0, 1, 2
 # distance functions (distanceFunctions.cuh:54-71)
@@ -390,7 +391,7 @@ __all__ = [
     "POINT_DTYPE", "Result", "LshgError", "calculate_k", "linear_scans", "LSH", "lsh", "random_normals",
     "random_plus_minus", "random_bools", "Index", "merge_topk", "validate", "parse_file", "write_file", "Server",
     "make_options", "launch_count", "profile_enable", "profile_report", "IMPL_EXACT", "IMPL_SIMHASH", "IMPL_WMH",
-    "IMPL_WMH_ONEBIT", "IMPL_JL", "IMPL_TC", "IMPL_TC_FP8", "IMPL_CWS", "KEYS_SIMHASH", "KEYS_WMH", "KEYS_WMH_ONEBIT", "KEYS_CROSSPOLY",
+    "IMPL_WMH_ONEBIT", "IMPL_JL", "IMPL_TC", "IMPL_TC_FP8", "IMPL_CWS", "KEYS_SIMHASH", "KEYS_WMH", "KEYS_WMH_ONEBIT", "KEYS_CROSSPOLY", "KEYS_CWS",
     "SKETCH_SCAN_AUTO", "SKETCH_SCAN_POPCOUNT", "SKETCH_SCAN_TENSOR",
     "ANGULAR", "JACCARD", "EUCLIDEAN", "EXPORT_DATA", "EXPORT_SKETCHES", "EXPORT_KEYS", "EXPORT_OFFSETS",
     "EXPORT_BUCKETS", "EXPORT_QUERY_COUNTERS", "EXPORT_CWS_CODES", "POINT_DTYPE", "read_truth", "write_truth",

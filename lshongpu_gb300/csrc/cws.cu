@@ -215,6 +215,30 @@ __global__ void cws_slice_kernel(const int2* __restrict__ smp, int64_t rows, int
   }
 }
 
+// LSH keys from CWS samples (keysImplementation 10): table t's key hashes its K samples
+// t K .. t K + K - 1 -- h = mix(h ^ (index << 32 | t)) per sample, from the table number,
+// with splitmix64's finaliser -- and keeps the top `bits` bits.  Equal samples give equal
+// keys, so two vectors share table t's bucket with probability at least J^K.
+__device__ __forceinline__ uint64_t key_mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void cws_keys_kernel(const int2* __restrict__ smp, int64_t rows, int L, int K, int bits,
+                                uint16_t* __restrict__ keys) {
+  const int64_t total = rows * L;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = w / L;
+    const int t = (int)(w - r * L);
+    uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(t + 1);
+    for (int j = 0; j < K; ++j) {
+      const int2 v = smp[r * (int64_t)L * K + (int64_t)t * K + j];
+      h = key_mix(h ^ (((uint64_t)(uint32_t)v.x << 32) | (uint32_t)v.y));
+    }
+    keys[w] = (uint16_t)(h >> (64 - bits));
+  }
+}
+
 struct DirectSmem {
   size_t qs, kept, buf, thr, cnt, total;
 };
@@ -346,25 +370,35 @@ static uint64_t cws_mix(uint64_t z) {
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
 }
-static double cws_uniform(int j, int i, int m) {
+static double cws_uniform(uint64_t seed, int j, int i, int m) {
   const uint64_t c = ((uint64_t)j * 65536u + (uint64_t)i) * 8u + (uint64_t)m;
-  const uint64_t z = cws_mix(kCwsSeed + (c + 1) * 0x9E3779B97F4A7C15ull);
+  const uint64_t z = cws_mix(seed + (c + 1) * 0x9E3779B97F4A7C15ull);
   return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);  // (0, 1)
 }
 
-void cws_tables(int d, int S, std::vector<float>& tab) {
+void cws_tables(int d, int S, std::vector<float>& tab, uint64_t seed) {
   tab.assign((size_t)d * S * 4, 0.0f);
   for (int i = 0; i < d; ++i)
     for (int j = 0; j < S; ++j) {
-      const double r = -(std::log(cws_uniform(j, i, 0)) + std::log(cws_uniform(j, i, 1)));  // Gamma(2, 1)
-      const double c = -(std::log(cws_uniform(j, i, 2)) + std::log(cws_uniform(j, i, 3)));
+      const double r = -(std::log(cws_uniform(seed, j, i, 0)) + std::log(cws_uniform(seed, j, i, 1)));  // Gamma(2, 1)
+      const double c = -(std::log(cws_uniform(seed, j, i, 2)) + std::log(cws_uniform(seed, j, i, 3)));
       const float rf = (float)r;
       float* t = &tab[((size_t)i * S + j) * 4];
       t[0] = rf;
       t[1] = 1.0f / rf;
       t[2] = (float)std::log(c);
-      t[3] = (float)cws_uniform(j, i, 4);
+      t[3] = (float)cws_uniform(seed, j, i, 4);
     }
+}
+
+void launch_cws_keys(const uint32_t* smp, int64_t rows, int L, int K, int bits, uint16_t* keys, cudaStream_t s) {
+  const int64_t total = rows * L;
+  if (total <= 0) return;
+  LSHG_REQUIRE(bits >= 1 && bits <= 16 && K >= 1, "CWS keys: bucketKeyBits in [1, 16], K >= 1");
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)num_sms() * 16);
+  cws_keys_kernel<<<blocks, 256, 0, s>>>(reinterpret_cast<const int2*>(smp), rows, L, K, bits, keys);
+  count_launch();
+  LSHG_CHECK_LAUNCH();
 }
 
 void launch_cws_sketch(const float* x, int64_t rows, int d, int S, const float* tab, uint32_t* out, cudaStream_t s) {

@@ -253,6 +253,13 @@ void make_keys(const Index& idx, const float* v, int64_t rows, DevBuf<uint16_t>*
     case 7:
       launch_crosspoly(v, rows, d, idx.cp_P, idx.tables, idx.cp_hashes, idx.cp_rounds, idx.cp_diag.ptr, keys->ptr, s);
       break;
+    case 10: {  // CWS samples, K a table, hashed into bucketKeyBits bits
+      const int S = idx.tables * idx.cp_hashes;
+      DevBuf<uint32_t> smp((size_t)rows * S * 2, s);
+      launch_cws_sketch(v, rows, d, S, idx.cws_key_tab.ptr, smp.ptr, s);
+      launch_cws_keys(smp.ptr, rows, idx.tables, idx.cp_hashes, idx.key_bits, keys->ptr, s);
+      break;
+    }
     default:
       throw Error(LSHG_ERR_INVALID_ARGUMENT, "invalid keysImplementation");
   }
@@ -317,7 +324,7 @@ Index::~Index() {
   sk_planes.release(); sk_split.release(); sk_pnorm.release();
   keys.release(); offsets.release(); buckets.release(); key_planes.release(); cp_diag.release(); bitmaps.release();
   xbf.release(); xbf_scale.release(); xf8.release(); xnorm64.release(); xst.release(); qstats.release();
-  cws_tab.release(); cws_rank.release();
+  cws_tab.release(); cws_rank.release(); cws_key_tab.release();
   for (auto* ops : {&ops_keys, &ops_sketch})
     for (auto& op : *ops)
       if (op.dminv) op.dminv->release();
@@ -414,6 +421,18 @@ std::unique_ptr<Index> build_index(const lshg_index_params& p, DevBuf<float>&& b
         wmh_prepare(I.wmh_keys, I.ops_keys, X, n, comp, nc, d, p.tables * p.bucketKeyBits, 1, p.tables,
                     p.bucketKeyBits, s);
         break;
+      case 10: {  // consistent weighted sampling keys, K = cp_hashes samples a table
+        LSHG_REQUIRE(p.bucketKeyBits <= 16, "CWS keys need bucketKeyBits <= 16");
+        LSHG_REQUIRE(d <= 4096, "CWS keys: d must be <= 4096");
+        I.cp_hashes = p.opt.cp_hashes > 0 ? p.opt.cp_hashes : 1;
+        LSHG_REQUIRE(I.cp_hashes <= 16, "CWS keys: at most 16 samples a table");
+        do_shift(I.ops_keys, X, n, comp, nc, d, s);  // the weighted MinHash preprocessing
+        do_normalize(I.ops_keys, X, n, comp, nc, d, s);
+        std::vector<float> tab;
+        cws_tables(d, p.tables * I.cp_hashes, tab, kCwsKeySeed);
+        upload(I.cws_key_tab, tab.data(), tab.size(), s);
+        break;
+      }
       case 7: {
         I.cp_P = log_dim(d);
         I.cp_hashes = p.opt.cp_hashes > 0 ? p.opt.cp_hashes : 1;

@@ -78,6 +78,7 @@ struct Index {
   DevBuf<int> offsets, buckets;
   DevBuf<float> key_planes;  // SimHash key planes [tables*bits][d]
   DevBuf<int> cp_diag;       // [tables][hashes][rounds][P]
+  DevBuf<float> cws_key_tab; // CWS keys (key kind 10): draw table [d][tables * cp_hashes][4]
   int cp_P = 0, cp_hashes = 1, cp_rounds = 3;
   WmhState wmh_keys;
   DevBuf<uint32_t> bitmaps;  // per-CTA dedupe bitmaps of the LSH query

@@ -104,7 +104,8 @@ void launch_byte_filter_scan(const uint32_t* xsl_t, const uint32_t* xst, int64_t
 
 // Consistent weighted sampling (implementation 10, cws.cu): (index, t) samples of the
 // generalized Jaccard similarity, their range-coded bit-sliced form, and the scan.
-constexpr uint64_t kCwsSeed = 0x6C7368672D637773ull;
+constexpr uint64_t kCwsSeed = 0x6C7368672D637773ull;     // sketch draws
+constexpr uint64_t kCwsKeySeed = 0x6C7368672D6B6579ull;  // LSH key draws (independent of the sketch's)
 struct CwsCodes {
   int tmin = 0, tmax = 0;  // range of t over the base's samples
   int kb = 0, tb = 0;      // code bits of the dimension index and of t - tmin
@@ -114,7 +115,10 @@ struct CwsCodes {
   const uint8_t* rank = nullptr;  // dictionaries [S][2^rlog] (device; owned by the index)
 };
 // Draw table [d][S] of (r, 1/r, ln c, beta) as 4 floats.
-void cws_tables(int d, int S, std::vector<float>& tab);
+void cws_tables(int d, int S, std::vector<float>& tab, uint64_t seed = kCwsSeed);
+// LSH keys [rows][L] from samples [rows][L * K]: table t hashes samples t K .. t K + K - 1
+// into `bits` bits.
+void launch_cws_keys(const uint32_t* smp, int64_t rows, int L, int K, int bits, uint16_t* keys, cudaStream_t s);
 // Samples of `rows` vectors: rows of S (index, t) int32 pairs (2 S words).
 void launch_cws_sketch(const float* x, int64_t rows, int d, int S, const float* tab, uint32_t* out, cudaStream_t s);
 // Code plan from the base's samples (synchronises the stream to read their range of t).

@@ -259,6 +259,10 @@ void check_loaded(const Reader& r, const Index& I) {
       case 5:
         check_wmh(r, I.wmh_keys, d, I.tables * I.key_bits, 1, I.tables, I.key_bits);
         break;
+      case 10:
+        need(I.key_bits <= 16 && I.cp_hashes >= 1 && I.cp_hashes <= 16 && d <= 4096, "CWS key shape");
+        need(r.count(&I.cws_key_tab) == (size_t)d * L * I.cp_hashes * 4, "CWS key draw table");
+        break;
       case 7: {
         int P = 1;
         while (P < d) P *= 2;
@@ -278,6 +282,7 @@ void check_loaded(const Reader& r, const Index& I) {
         bad("key kind");
     }
     if (I.key_kind != 4 && I.key_kind != 5) check_no_wmh(r, I.wmh_keys);
+    if (I.key_kind != 10) need(!r.count(&I.cws_key_tab), "key buffers");
     need(r.count(&I.key_planes) == kp && r.count(&I.cp_diag) == diag, "key buffers");
     // offsets ascend within a table's region [t*n, t*n + n]; ids are row numbers
     const int32_t* off = r.data(I.offsets);
@@ -293,7 +298,7 @@ void check_loaded(const Reader& r, const Index& I) {
     for (size_t i = 0; i < L * (size_t)n; ++i) need(bk[i] >= 0 && bk[i] < n, "bucket ids");
   } else {
     need(I.key_kind == 0 && !r.count(&I.keys) && !r.count(&I.offsets) && !r.count(&I.buckets) &&
-             !r.count(&I.key_planes) && !r.count(&I.cp_diag),
+             !r.count(&I.key_planes) && !r.count(&I.cp_diag) && !r.count(&I.cws_key_tab),
          "bucket tables");
     check_no_wmh(r, I.wmh_keys);
   }
@@ -345,6 +350,7 @@ void buffers_io(IO& io, Index& I, cudaStream_t s) {
   io.dev(I.xbf_scale, s);
   io.dev(I.xf8, s);
   io.dev(I.cws_tab, s);
+  io.dev(I.cws_key_tab, s);
   wmh_io(io, I.wmh_sk, s);
   wmh_io(io, I.wmh_keys, s);
 }

@@ -33,6 +33,8 @@ _SIGS = {
     "or_wmh_bounds": (i32, [P, i64, P, i64, i32, P, P, i32]),
     "or_wmh_sketch": (i64, [P, i64, i32, P, P, i32, P, i32, i32, i32, i32, i32, P, i32, P, P]),
     "or_cws_tables": (None, [i32, i32, P]),
+    "or_cws_tables_seeded": (None, [i32, i32, i32, P]),
+    "or_cws_keys": (None, [P, i64, i32, i32, i32, P]),
     "or_cws_logf": (C.c_float, [C.c_float]),
     "or_cws_sketch": (None, [P, i64, i32, i32, P, P]),
     "or_sketch_scan": (None, [P, i64, P, i64, i32, i32, P, P, i32, i32, i32, i32, P, P, P]),
@@ -170,6 +172,22 @@ def cws_tables(d, S):
     """Consistent weighted sampling draw table [d][S][4]: r, 1/r, ln c, beta."""
     out = np.empty((d, S, 4), np.float32)
     lib().or_cws_tables(d, S, _p(out))
+    return out
+
+
+def cws_key_tables(d, S):
+    """Draw table of CWS LSH keys (keysImplementation 10), [d][S][4]."""
+    out = np.empty((d, S, 4), np.float32)
+    lib().or_cws_tables_seeded(d, S, 1, _p(out))
+    return out
+
+
+def cws_keys(x, L, K, bits):
+    """CWS LSH keys [n][L] u16 of preprocessed rows x: L * K samples hashed K a table."""
+    x = _f32(x)
+    smp = cws_sketch(x, L * K, cws_key_tables(x.shape[1], L * K))
+    out = np.empty((x.shape[0], L), np.uint16)
+    lib().or_cws_keys(_p(smp), x.shape[0], L, K, bits, _p(out))
     return out
 
 

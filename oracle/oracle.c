@@ -439,24 +439,44 @@ static uint64_t cws_mix(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-static double cws_uniform(int j, int i, int m) {
+#define CWS_KEY_SEED 0x6C7368672D6B6579ull
+
+static double cws_uniform(uint64_t seed, int j, int i, int m) {
   uint64_t c = ((uint64_t)j * 65536u + (uint64_t)i) * 8u + (uint64_t)m;
-  uint64_t z = cws_mix(CWS_SEED + (c + 1) * 0x9E3779B97F4A7C15ull);
+  uint64_t z = cws_mix(seed + (c + 1) * 0x9E3779B97F4A7C15ull);
   return ((double)(z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
 
-/* table [d][S][4]: r, 1/r, ln c, beta (r, c ~ Gamma(2, 1) as sums of two Exp(1)) */
-void or_cws_tables(int d, int S, float* tab) {
+/* table [d][S][4]: r, 1/r, ln c, beta (r, c ~ Gamma(2, 1) as sums of two Exp(1));
+ * key = 1: the draws of LSH keys (keysImplementation 10), independent of the sketch's */
+void or_cws_tables_seeded(int d, int S, int key, float* tab) {
+  const uint64_t seed = key ? CWS_KEY_SEED : CWS_SEED;
   for (int i = 0; i < d; ++i)
     for (int j = 0; j < S; ++j) {
-      double r = -(log(cws_uniform(j, i, 0)) + log(cws_uniform(j, i, 1)));
-      double c = -(log(cws_uniform(j, i, 2)) + log(cws_uniform(j, i, 3)));
+      double r = -(log(cws_uniform(seed, j, i, 0)) + log(cws_uniform(seed, j, i, 1)));
+      double c = -(log(cws_uniform(seed, j, i, 2)) + log(cws_uniform(seed, j, i, 3)));
       float rf = (float)r;
       float* t = tab + ((size_t)i * S + j) * 4;
       t[0] = rf;
       t[1] = 1.0f / rf;
       t[2] = (float)log(c);
-      t[3] = (float)cws_uniform(j, i, 4);
+      t[3] = (float)cws_uniform(seed, j, i, 4);
+    }
+}
+void or_cws_tables(int d, int S, float* tab) { or_cws_tables_seeded(d, S, 0, tab); }
+
+/* LSH keys [n][L] from samples [n][L*K][2]: table t folds its K samples into a 64-bit
+ * hash (h = mix(h ^ (index << 32 | t)), starting from golden * (t + 1)) and keeps the top
+ * `bits` bits. */
+void or_cws_keys(const int32_t* smp, int64_t n, int L, int K, int bits, uint16_t* keys) {
+  for (int64_t r = 0; r < n; ++r)
+    for (int t = 0; t < L; ++t) {
+      uint64_t h = 0x9E3779B97F4A7C15ull * (uint64_t)(t + 1);
+      for (int j = 0; j < K; ++j) {
+        const int32_t* v = smp + ((r * L + t) * (int64_t)K + j) * 2;
+        h = cws_mix(h ^ (((uint64_t)(uint32_t)v[0] << 32) | (uint32_t)v[1]));
+      }
+      keys[r * L + t] = (uint16_t)(h >> (64 - bits));
     }
 }
 

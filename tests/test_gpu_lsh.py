@@ -254,3 +254,46 @@ def test_wmh_byte_keys_need_256_buckets(engine):
     x = datasets.sparse_gamma(200, D, 5)
     with pytest.raises(engine.LshgError):
         engine.Index(x, implementation=2, distanceFunc=2, framework=1, keysImplementation=4, bucketKeyBits=7, tables=4)
+
+
+@pytest.mark.parametrize("K,bits,dist", [(1, 10, 2), (2, 12, 2), (3, 8, 1)])
+def test_cws_keys_buckets_query(engine, orc, K, bits, dist):
+    """Consistent-weighted-sampling keys (keysImplementation 10; K samples a table hashed
+    into bucketKeyBits bits): base and query keys bit-exact against the oracle, bucket
+    offsets and contents equal, query results equal -- through the resident index and
+    the reference-shaped LSH() entry point; a save/load round trip answers alike."""
+    import os
+    import tempfile
+
+    n, nq, L = 4000, 16, 8
+    x = datasets.sparse_gamma(n, D, 301 + bits)
+    q = datasets.sparse_gamma(nq, D, 401 + bits)
+    S = 1 << bits
+    opt = engine.make_options(cp_hashes=K)
+    idx = engine.Index(x, implementation=2, distanceFunc=dist, framework=1, keysImplementation=10,
+                       bucketKeyBits=bits, tables=L, options=opt)
+    xs = orc.normalize(x)  # nonnegative data: the recorded shift is zero
+    qs = orc.normalize(q)
+    okeys = orc.cws_keys(xs, L, K, bits)
+    keys, off, bk = lsh_index_arrays(engine, idx, n, L, S)
+    assert np.array_equal(keys, okeys)
+    ooff, obk = orc.lsh_build(okeys, L, S)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(bk, obk)
+    oqk = orc.cws_keys(qs, L, K, bits)
+    _, qk = idx.sketch_queries(q, np.uint32, 0, L)
+    assert np.array_equal(qk, oqk)
+    res = idx.query(q, 32)
+    ids, ds = orc.lsh_query(xs, qs, oqk, L, S, ooff, obk, 0, 0, None, None, 0, 32, dist, 32)
+    assert np.array_equal(res["ID"], ids)
+    assert np.array_equal(res["distance"], ds)
+    assert (ids[:, 0] >= 0).all()
+
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "cws_keys.lshg")
+        idx.save(path)
+        assert np.array_equal(engine.Index.load(path).query(q, 32), res)
+
+    r = engine.LSH(2, 10, 32, D, nq, n, x, q, 0, dist, bits, L, False, options=opt)
+    assert np.array_equal(r.ids, ids)
+    assert np.array_equal(r.distances, ds)
