@@ -9,7 +9,9 @@ the CPU oracle to scan the whole batch.
   consistent weighted sampling (500k sparse Gamma rows, 256 samples, C = 4,096): the
   results of a few queries of a full batch equal the oracle's scan of the index's own
   sketches (exact top-C by sketch distance, then the exact re-rank), and for CWS a sample
-  of base rows' (index, t) pairs equals the oracle's sampler.
+  of base rows' (index, t) pairs equals the oracle's sampler;
+* cross-polytope LSH (1M x 128, L = 32, K = 2): queries of a full batch equal the oracle's
+  bucket walk over the index's own keys and bucket tables.
 """
 import os
 
@@ -87,5 +89,26 @@ def test_weighted_minhash_full_size(engine, orc, impl):
         assert np.array_equal(skx[rows], orc.cws_sketch(xp[rows], S, tab))
         assert np.array_equal(skq, orc.cws_sketch(qp, S, tab))
     ids, ds = orc.sketch_scan(xp, qp, impl, skx, skq, S, C, 2, 32)
+    assert np.array_equal(res["ID"][pick], ids)
+    assert np.array_equal(res["distance"][pick], ds)
+
+
+def test_crosspoly_lsh_full_size(engine, orc):
+    """Configuration 4a (1M x 128 with 28 zero dimensions, L = 32 tables of K = 2
+    cross-polytope hashes): for queries of a full batch, the results equal the oracle's
+    bucket walk over the index's own keys and bucket tables."""
+    n, nq, L, bits = 1_000_000, 1024, 32, 16
+    x = datasets.clustered(n, D, 100, pad_to=128)
+    q = datasets.clustered(nq, D, 101, pad_to=128)
+    idx = engine.Index(x, implementation=2, distanceFunc=1, framework=1, keysImplementation=7, bucketKeyBits=bits,
+                       tables=L, options=engine.make_options(cp_hashes=2))
+    res = idx.query(q, 32)
+    S = 1 << bits
+    off = np.frombuffer(idx.export(engine.EXPORT_OFFSETS), np.int32)
+    bk = np.frombuffer(idx.export(engine.EXPORT_BUCKETS), np.int32)
+    xp = np.frombuffer(idx.export(engine.EXPORT_DATA), np.float32).reshape(n, 128)  # normalised for the keys
+    pick = np.array([0, 500, 1023])
+    _, qk = idx.sketch_queries(q[pick], np.uint32, 0, L)
+    ids, ds = orc.lsh_query(xp, orc.normalize(q[pick]), qk, L, S, off, bk, 0, 0, None, None, 0, 32, 1, 32)
     assert np.array_equal(res["ID"][pick], ids)
     assert np.array_equal(res["distance"][pick], ds)
