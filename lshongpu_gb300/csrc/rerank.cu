@@ -25,6 +25,7 @@ namespace lshg {
 namespace {
 
 constexpr int kBandMax = 128;  // entries a query's FP64 re-check covers at most
+constexpr uint64_t kPartitionBytes = 32ull << 20;  // base rows above this: gather in base order
 
 // Double-precision closeness of a float row to the query as a ratio a / b (larger =
 // closer, b > 0), computed by a whole warp: lane l sums the terms of dimensions l, l + 32,
@@ -302,21 +303,67 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
   }
 }
 
+// Candidate lists in base order, for the gather below: each query's C keys are
+// partitioned into B = C / 128 ranges of ids (range = id * B / n), empty and out-of-range
+// entries last.  The gather's grid runs chunk-major (every query's first chunk of 128,
+// then every query's second, ...), so the CTAs in flight at one time read rows from about
+// one range, 1 / B of the base; that range stays in L2 while every query's candidates in
+// it are scored, and a base larger than L2 is read from DRAM about once a batch instead of
+// once a candidate.  The order inside a range is the order of shared-memory atomics; the
+// re-rank's result does not depend on it (its keys are ordered by (distance, id)).
+constexpr int kPartPer = 8;  // keys a thread; C <= 512 * kPartPer
+__global__ void __launch_bounds__(512) cand_partition_kernel(const uint64_t* __restrict__ cand, int C, int64_t n,
+                                                             uint64_t* __restrict__ out) {
+  __shared__ int cnt[4096 / 128 + 1];
+  const int B = C / 128, qi = blockIdx.x;
+  for (int b = threadIdx.x; b <= B; b += blockDim.x) cnt[b] = 0;
+  __syncthreads();
+  uint64_t v[kPartPer];
+  int at[kPartPer];  // range << 16 | place in the range
+#pragma unroll
+  for (int e = 0; e < kPartPer; ++e) {
+    const int i = e * blockDim.x + threadIdx.x;
+    at[e] = -1;
+    if (i < C) {
+      v[e] = cand[(int64_t)qi * C + i];
+      const int id = key_id(v[e]);
+      const int r = (v[e] != kEmptyKey && id >= 0 && id < n) ? (int)(((int64_t)id * B) / n) : B;
+      at[e] = (r << 16) | atomicAdd(&cnt[r], 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int b = 0; b <= B; ++b) {
+      const int c = cnt[b];
+      cnt[b] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < kPartPer; ++e)
+    if (at[e] >= 0) out[(int64_t)qi * C + cnt[at[e] >> 16] + (at[e] & 0xffff)] = v[e];
+}
+
 // Long candidate lists (C >= 1024) in two kernels: the gather kernel scores one chunk of
 // blockDim candidates of one query a CTA (rows staged by bulk copies as above) and writes
 // their keys; small CTAs with nothing but the gather keep several chunks in flight an SM,
-// where one CTA a query walking all its chunks in turn waited on each.  The select kernel
-// then sorts each query's keys, applies the FP64 re-check and writes the first k.
+// where one CTA a query walking all its chunks in turn waited on each.  The grid is
+// (query, chunk) with the query fastest, so with lists in base order (above) the CTAs in
+// flight share one range of the base.  cand and keys_out may be the same buffer: each
+// thread reads its entry before it writes it.  The select kernel then sorts each query's
+// keys, applies the FP64 re-check and writes the first k.
 template <int DIST>
-__global__ void rerank_gather_kernel(const uint64_t* __restrict__ cand, int C, const float* __restrict__ x, int64_t n,
+__global__ void rerank_gather_kernel(const uint64_t* cand, int C, const float* __restrict__ x, int64_t n,
                                      int d, const float* __restrict__ xnorm, const float* __restrict__ q,
-                                     const float* __restrict__ qnorm, uint64_t* __restrict__ keys_out, int* err) {
+                                     const float* __restrict__ qnorm, uint64_t* keys_out, int* err) {
   extern __shared__ __align__(128) unsigned char rsm[];
   const int CH = blockDim.x;
   const uint32_t slot = stage_slot_bytes(d), rowb = (uint32_t)d * 4u;
   float* qr = reinterpret_cast<float*>(rsm + (size_t)CH * slot);
   __shared__ __align__(8) uint64_t bar;
-  const int qi = blockIdx.y, tid = threadIdx.x, i = blockIdx.x * CH + tid;
+  const int qi = blockIdx.x, tid = threadIdx.x, i = blockIdx.y * CH + tid;
   const uint32_t bar_a = tc::smem_u32(&bar);
   if (tid == 0) tc::mbar_init(bar_a, 1);
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -517,11 +564,20 @@ void launch_rerank(const uint64_t* cand, int nq, int C, const float* x, int64_t 
   const size_t select_smem = (size_t)C * 8 + (size_t)d * 4 + 16;
   if (stageable && C >= 1024 && !test_stall && gather_smem <= 96 * 1024 && select_smem <= 200 * 1024) {
     DevBuf<uint64_t> gk((size_t)nq * C, s);
+    // lists in base order when the rows do not fit in a quarter of L2 (the gather then
+    // reads them in place)
+    const uint64_t* gin = cand;
+    if (C <= 512 * kPartPer && (uint64_t)n * (uint64_t)d * 4u > kPartitionBytes) {
+      cand_partition_kernel<<<nq, 512, 0, s>>>(cand, C, n, gk.ptr);
+      count_launch();
+      LSHG_CHECK_LAUNCH();
+      gin = gk.ptr;
+    }
 #define LSHG_RR2(DV)                                                                                            \
   do {                                                                                                          \
     LSHG_CUDA(cudaFuncSetAttribute(rerank_gather_kernel<DV>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
                                    (int)gather_smem));                                                          \
-    rerank_gather_kernel<DV><<<dim3(C / 128, nq), 128, gather_smem, s>>>(cand, C, x, n, d, xnorm, q, qnorm,     \
+    rerank_gather_kernel<DV><<<dim3(nq, C / 128), 128, gather_smem, s>>>(gin, C, x, n, d, xnorm, q, qnorm,      \
                                                                          gk.ptr, err);                          \
     count_launch();                                                                                             \
     LSHG_CHECK_LAUNCH();                                                                                        \
