@@ -483,6 +483,46 @@ int lshg_validate(const lshg_point* truth, int truth_k, const lshg_point* result
 }
 
 // ---- reference text format (gloveparser.cu:9-86; DataParsing/Writer/writer.cpp) --
+//
+// A file is a line with n, a line with d, then a line a point: "<id> v v ... v " with a
+// space after every value.  Values are read by the reference reader's rules, kept because
+// existing files (and the ground truth computed from them) went through that reader:
+//   * the first space-separated field of a line (the id) is skipped;
+//   * a value is stored when the space after it is read: a field that ends its line or
+//     the file is dropped, and two spaces in a row store a zero;
+//   * in a value field only '0'-'9', '-' and '.' count, every other byte is skipped:
+//       - a digit before any '.' replaces the value ("12.5" reads 2.5, "1e3" reads 3);
+//       - every '.' and every digit after one advance a place count e, and such a digit c
+//         adds c / 10^e, in double, to the float value ("1.2.3" reads 1.203);
+//       - a '-' anywhere in the field negates the stored value; the sign is cleared only
+//         when a value is stored, so the '-' of a dropped field at a line end carries over
+//         to the next stored value.
+
+namespace {
+
+// Value of one field by the rules above; `neg` is set by a '-' and left set otherwise.
+float field_value(const unsigned char* b, const unsigned char* e, bool& neg) {
+  float v = 0.0f;
+  int places = 0;  // 0: no '.' seen yet
+  for (; b < e; ++b) {
+    const unsigned c = *b;
+    if (c >= '0' && c <= '9') {
+      if (places == 0) {
+        v = (float)(c - 48.0);
+      } else {
+        v = (float)(v + (c - 48.0) / std::pow(10.0, (double)places));
+        ++places;
+      }
+    } else if (c == '-') {
+      neg = true;
+    } else if (c == '.') {
+      ++places;
+    }
+  }
+  return v;
+}
+
+}  // namespace
 
 int lshg_parse_file(const char* path, int* n_out, int* d_out, float** out) {
   return guarded([&] {
@@ -494,60 +534,40 @@ int lshg_parse_file(const char* path, int* n_out, int* d_out, float** out) {
       fclose(fp);
       throw Error(LSHG_ERR_IO, "truncated header");
     }
-    int n = atoi(nb), d = atoi(db);
+    const int n = atoi(nb), d = atoi(db);
     if (n < 0 || d <= 0) {
       fclose(fp);
       throw Error(LSHG_ERR_IO, "bad header");
     }
-    float* list = (float*)calloc((size_t)n * d + 1, sizeof(float));
-    // Same character machine as the reference: the first token of a line is the ID; a
-    // value is committed at each space; only the last digit before the point is kept;
-    // fraction digits accumulate as double added to a float.
-    bool neg = false, comma = false, isID = true;
-    int comma_counter = 0;
-    size_t index = 0, cap = (size_t)n * d;
-    float x = 0;
-    int ch;
-    while ((ch = fgetc(fp)) != EOF) {
-      while (ch != 10 && ch != EOF) {
-        if (ch == 32) {
-          if (isID) {
-            isID = false;
-          } else {
-            if (neg) x = x * -1.0;
-            if (index < cap) list[index] = x;
-            x = 0;
-            index++;
-            comma = false;
-            neg = false;
-            comma_counter = 0;
-          }
-        } else if (isID) {
-        } else if (ch >= '0' && ch <= '9') {
-          if (comma) {
-            double digit = (ch - 48.0) / pow(10, comma_counter);
-            x = x + digit;
-            comma_counter++;
-          } else {
-            x = ch - 48.0;
-          }
-        } else if (ch == 45) {
-          neg = true;
-        } else if (ch == 46) {
-          comma = true;
-          comma_counter++;
-        }
-        ch = fgetc(fp);
-      }
-      x = 0;
-      comma = false;
-      comma_counter = 0;
-      isID = true;
-    }
+    std::vector<unsigned char> text;
+    unsigned char chunk[1 << 16];
+    for (size_t got; (got = fread(chunk, 1, sizeof chunk, fp)) > 0;) text.insert(text.end(), chunk, chunk + got);
     fclose(fp);
+    const size_t cap = (size_t)n * d;
+    float* vals = (float*)calloc(cap + 1, sizeof(float));
+    if (!vals) throw Error(LSHG_ERR_OUT_OF_MEMORY, "cannot allocate the dataset");
+    const unsigned char* t = text.data();
+    const unsigned char* end = t + text.size();
+    size_t stored = 0;
+    bool neg = false;
+    for (const unsigned char* line = t; line < end;) {
+      const unsigned char* eol = std::find(line, end, (unsigned char)'\n');
+      const unsigned char* f = std::find(line, eol, (unsigned char)' ');  // end of the id
+      while (f < eol) {
+        const unsigned char* b = f + 1;
+        f = std::find(b, eol, (unsigned char)' ');
+        float v = field_value(b, f, neg);
+        if (f == eol) break;  // no space after the field: dropped
+        if (neg) v = -v;
+        neg = false;
+        if (stored < cap) vals[stored] = v;
+        ++stored;
+      }
+      line = eol + 1;
+    }
     *n_out = n;
     *d_out = d;
-    *out = list;
+    *out = vals;
   });
 }
 

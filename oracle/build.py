@@ -4,6 +4,7 @@ the reference's own CPU code under oracle/_ref/.
   oracle/build/liboracle.so   oracle.c + gold_port.cpp (gcc/g++, -ffp-contract=off)
   oracle/_ref/rng_driver      LinearScan/randomVectorGenerator.cpp + ref_drivers/rng_driver.cpp
   oracle/_ref/goldstandard    GoldStandard/goldstandard.cpp, unmodified
+  oracle/_ref/parse_driver    LinearScan/gloveparser.cu (host code, nvcc) + ref_drivers/parse_driver.cpp
 
 The reference sources are compiled where they lie (read-only); nothing of them is
 copied into this repository.  Outputs of the reference build go to oracle/_ref only.
@@ -62,6 +63,16 @@ def build_reference() -> list[str]:
     gs = os.path.join(REF_OUT, "goldstandard")
     _run(["g++", "-O2", "-std=c++11", "-o", gs, os.path.join(REFERENCE, "GoldStandard", "goldstandard.cpp")])
     outs.append(gs)
+    # the text reader is host code in a .cu file that includes thrust: nvcc for it, g++
+    # for the driver, nvcc to link
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    gp_obj = os.path.join(REF_OUT, "gloveparser.o")
+    pd_obj = os.path.join(REF_OUT, "parse_driver.o")
+    pd = os.path.join(REF_OUT, "parse_driver")
+    _run([nvcc, "-O2", "-std=c++17", "-w", "-c", os.path.join(ls, "gloveparser.cu"), "-o", gp_obj])
+    _run(["g++", "-O2", "-c", os.path.join(HERE, "ref_drivers", "parse_driver.cpp"), "-o", pd_obj])
+    _run([nvcc, gp_obj, pd_obj, "-o", pd])
+    outs.append(pd)
     return outs
 
 

@@ -111,6 +111,25 @@ def test_text_format_roundtrip_and_quirks(engine):
         assert z[1, 1:].tolist() == [7.0, -0.5]
 
 
+def test_text_reader_matches_reference_reader(engine, tmp_path):
+    """The reader against the reference's parseFile (LinearScan/gloveparser.cu), run on
+    the same files by tests/golden/make_golden.py: writer output, multi-digit integer
+    parts, exponents, repeated points, inner '-', other bytes, double spaces, CR line
+    ends, long fractions, an empty id, an empty line, a dropped '-' field carrying its
+    sign to the next line, and a file without a final newline -- bit for bit."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "text_reader.npz"))
+    toff = voff = 0
+    for i, (ln, (n, d)) in enumerate(zip(z["text_len"], z["shape"])):
+        p = tmp_path / f"case{i}.txt"
+        p.write_bytes(z["text"][toff:toff + ln].tobytes())
+        want = z["values"][voff:voff + n * d].reshape(n, d)
+        toff += ln
+        voff += n * d
+        got = engine.parse_file(str(p))
+        assert got.shape == (n, d)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), i
+
+
 def _free_port():
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
