@@ -228,8 +228,6 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
     tc::mbar_init(never_a, 1);
   }
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
-  __syncthreads();
   const float qn = (DIST == DIST_ANGULAR) ? qnorm[qi] : 1.0f;
   unsigned char* dst = stage + (size_t)tid * slot;
   uint32_t phase = 0, pending = 0;
@@ -251,6 +249,12 @@ __global__ void rerank_staged_kernel(const uint64_t* __restrict__ cand, int nq, 
       if (tid == 0) tc::mbar_expect_tx(bar_a, (uint32_t)nv * rowb);
       __syncthreads();
       if (id >= 0) tc::bulk_load(tc::smem_u32(dst), x + (int64_t)id * d, rowb, bar_a);
+    }
+    // the query row while the first chunk's rows are in flight; published by the barrier
+    // that ends this chunk's wait (or the next chunk's count when this one has no rows)
+    if (c0 == 0)
+      for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
+    if (ok && nv > 0) {
       const bool stall = test_stall && c0 == 0;
       const uint32_t wbar = stall ? never_a : bar_a;
       const uint64_t limit = stall ? 1000000ull : tc::kWaitNs;
@@ -367,7 +371,6 @@ __global__ void rerank_gather_kernel(const uint64_t* cand, int C, const float* _
   const uint32_t bar_a = tc::smem_u32(&bar);
   if (tid == 0) tc::mbar_init(bar_a, 1);
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
   int id = -1;
   if (i < C) {
     const uint64_t kin = cand[(int64_t)qi * C + i];
@@ -385,6 +388,8 @@ __global__ void rerank_gather_kernel(const uint64_t* cand, int C, const float* _
     if (tid == 0) tc::mbar_expect_tx(bar_a, (uint32_t)nv * rowb);
     __syncthreads();
     if (id >= 0) tc::bulk_load(tc::smem_u32(dst), x + (int64_t)id * d, rowb, bar_a);
+    // the query row while the candidate rows are in flight (published by the barrier below)
+    for (int j = tid; j < d; j += CH) qr[j] = q[(int64_t)qi * d + j];
     bool got = tc::mbar_try(bar_a, 0);
     if (!got) {
       const uint64_t t0 = tc::global_ns();

@@ -69,7 +69,7 @@ struct FLayout {
   static constexpr int BAR_OFF = S_OFF + 4 * F_SBUF * BM * 8;
   static constexpr int SMEM = BAR_OFF + 256 + 1024;           // + barriers + 1 KB alignment slack
   static_assert(SMEM <= 232448, "shared memory per CTA");
-  static_assert(8 * (2 * STAGES + 5 + 2 * F_NACC) + 8 <= 256, "barrier area");
+  static_assert(8 * (4 * STAGES + 5 + 2 * F_NACC) + 8 <= 256, "barrier area");
 };
 
 struct FilterArgs {
@@ -128,7 +128,15 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   auto ACC_FULL = [&](int b) { return bar0 + 8u * (2 * F_STAGES + 4 + b); };
   auto ACC_EMPTY = [&](int b) { return bar0 + 8u * (2 * F_STAGES + 4 + F_NACC + b); };
   const uint32_t DONE = bar0 + 8u * (2 * F_STAGES + 4 + 2 * F_NACC);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + F_BAR_OFF + 8 * (2 * F_STAGES + 5 + 2 * F_NACC));
+  // Prepass (BF16): the second 64-column half of a base stage has barriers of its own
+  // (FULL / EMPTY cover the first), so the first half is refilled once its four K steps
+  // are done.  The prepass reads every S-th tile and its epilogue is light, so it waits on
+  // the copies: split, it ran 16% faster at 1.2M x 100.  The filter pass ran 6% slower
+  // split and keeps one pair of barriers a stage.
+  constexpr bool SPLIT = !F8 && MODE == MODE_GROUPMAX;
+  auto FULL_HI = [&](int s) { return bar0 + 8u * (2 * F_STAGES + 5 + 2 * F_NACC + s); };
+  auto EMPTY_HI = [&](int s) { return bar0 + 8u * (3 * F_STAGES + 5 + 2 * F_NACC + s); };
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + F_BAR_OFF + 8 * (4 * F_STAGES + 5 + 2 * F_NACC));
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
@@ -138,6 +146,8 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     for (int s = 0; s < F_STAGES; ++s) {
       mbar_init(FULL(s), 1);
       mbar_init(EMPTY(s), 1);
+      mbar_init(FULL_HI(s), 1);
+      mbar_init(EMPTY_HI(s), 1);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(A_FULL(s), 1);
@@ -161,7 +171,7 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       int it = 0, ua = 0;
-      bool ok = true;
+      bool ok = true, last_hi = true;  // last_hi: the last tile's second half was issued
       for (int u = blockIdx.x; u < U && ok; u += gridDim.x, ++ua) {
         const int qt = u % a.QT, c = u / a.QT;
         const int p0 = c * a.CH, p1 = min(a.NP, p0 + a.CH);
@@ -178,17 +188,29 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           if (F8) {
             mbar_expect_tx(FULL(st), B_TILE);
             tma_load_2d(dst, &mapB, 0, row, FULL(st));
-          } else {
+          } else if (!SPLIT) {
             mbar_expect_tx(FULL(st), B_HALF + TN * a.hi_cols * 2);
             tma_load_2d(dst, &mapB, 0, row, FULL(st));
             tma_load_2d(dst + B_HALF, &mapBhi, KHALF, row, FULL(st));
+          } else {
+            mbar_expect_tx(FULL(st), B_HALF);
+            tma_load_2d(dst, &mapB, 0, row, FULL(st));
+            if (!mbar_wait(EMPTY_HI(st), (rd & 1) ^ 1, abort_flag)) { ++it; last_hi = false; ok = false; break; }
+            mbar_expect_tx(FULL_HI(st), TN * a.hi_cols * 2);
+            tma_load_2d(dst + B_HALF, &mapBhi, KHALF, row, FULL_HI(st));
           }
           ++it;
         }
       }
-      // drain: every issued copy has landed before the CTA may exit
-      for (int j = max(0, it - F_STAGES); j < it; ++j)
-        mbar_wait(FULL(j % F_STAGES), (j / F_STAGES) & 1, abort_flag, true);
+      // drain: every issued copy has landed before the CTA may exit -- the last F_STAGES
+      // tiles.  Split stages: the second halves too, except the last tile's when it was
+      // never issued; then the second half of the tile before the window may still be in
+      // flight (only its first half's MMAs had to finish before the last tile was issued)
+      for (int j = max(0, it - F_STAGES - 1); j < it; ++j) {
+        if (j >= it - F_STAGES) mbar_wait(FULL(j % F_STAGES), (j / F_STAGES) & 1, abort_flag, true);
+        if (SPLIT && (last_hi ? j >= it - F_STAGES : j < it - 1))
+          mbar_wait(FULL_HI(j % F_STAGES), (j / F_STAGES) & 1, abort_flag, true);
+      }
       for (int j = max(0, ua - 2); j < ua; ++j) mbar_wait(A_FULL(j & 1), (j >> 1) & 1, abort_flag, true);
     }
     __syncwarp();
@@ -210,13 +232,22 @@ __global__ void __launch_bounds__(F_THREADS, 1)
           const int st = it % F_STAGES, rd = it / F_STAGES;
           if (!mbar_wait(FULL(st), rd & 1, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          if (F8)
-            umma_tile_e4m3<TN>(tmem + (uint32_t)(b * TN), s0 + F_A_OFF + ab * A_BYTES, s0 + F_B_OFF + st * B_TILE,
-                               a.ksteps);
-          else
-            umma_tile<TN>(tmem + (uint32_t)(b * TN), s0 + F_A_OFF + ab * A_BYTES, s0 + F_B_OFF + st * B_TILE,
-                          a.ksteps);
-          umma_commit(EMPTY(st));
+          const uint32_t dt = tmem + (uint32_t)(b * TN), as = s0 + F_A_OFF + ab * A_BYTES;
+          const uint32_t bs = s0 + F_B_OFF + st * B_TILE;
+          if (F8) {
+            umma_tile_e4m3<TN>(dt, as, bs, a.ksteps);
+            umma_commit(EMPTY(st));
+          } else if (!SPLIT) {
+            umma_tile<TN>(dt, as, bs, a.ksteps);
+            umma_commit(EMPTY(st));
+          } else {
+            umma_steps<TN>(dt, as, bs, 0, min(4, a.ksteps));
+            umma_commit(EMPTY(st));
+            if (!mbar_wait(FULL_HI(st), rd & 1, abort_flag)) { ok = false; break; }
+            tc_fence_after();
+            umma_steps<TN>(dt, as, bs, 4, a.ksteps);
+            umma_commit(EMPTY_HI(st));
+          }
           umma_commit(ACC_FULL(b));
           ++it;
         }

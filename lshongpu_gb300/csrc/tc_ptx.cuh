@@ -129,6 +129,20 @@ __device__ __forceinline__ void umma_tile(uint32_t d_tmem, uint32_t a_base, uint
     }
   }
 }
+// K steps [k0, k1) of umma_tile: a tile's MMAs issued in pieces, each after its own part
+// of the operands has landed.  Step 0 clears the accumulator.
+template <int N>
+__device__ __forceinline__ void umma_steps(uint32_t d_tmem, uint32_t a_base, uint32_t b_base, int k0, int k1) {
+  constexpr uint32_t idesc = idesc_bf16(BM, N);
+#pragma unroll
+  for (int kk = 0; kk < KD / 16; ++kk) {
+    if (kk >= k0 && kk < k1) {
+      const uint32_t koff = (kk & 3) * 32;
+      umma_bf16(d_tmem, smem_desc(a_base + (kk >> 2) * HALF_BYTES + koff),
+                smem_desc(b_base + (kk >> 2) * (N * 128) + koff), idesc, kk > 0 ? 1u : 0u);
+    }
+  }
+}
 __host__ __device__ inline int tc_ksteps(int d) { return d <= 0 ? 1 : (d > KD ? KD / 16 : (d + 15) / 16); }
 
 // FP8 operands: rows of KD E4M3 bytes (one 128-byte swizzle row holds the whole K).
