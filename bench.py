@@ -38,6 +38,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -101,6 +102,10 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            # the timed region starts once the sampler has written its first sample
+            t0 = time.perf_counter()
+            while os.path.getsize(self.path) == 0 and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
@@ -372,6 +377,8 @@ def run_reference_arm(args, world, rank):
 
     if rank != 0:
         return
+    if args.steps is None:
+        args.steps = 5
     x, q = make_data(0)
     threads = os.cpu_count() or 1
     sample = max(threads, min(N_QUERY, 2 * threads))
@@ -405,7 +412,8 @@ def run_reference_arm(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: about one second of timed work, at least 5; the reference arm: 5)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--path", default=None, choices=["tc", "tc8", "exact", "simhash", "cplsh", "wmh", "wmh1", "cws"])
@@ -470,10 +478,19 @@ def main():
     def step():
         idx.query_device_async(qd.data_ptr(), N_QUERY, K, out.data_ptr(), stream=sh)
 
+    tw = time.perf_counter()
     for _ in range(args.warmup):
         step()
     idx.sync(sh)
     torch.cuda.synchronize()
+    if args.steps is None:
+        # about one second of timed work, so that the clock sampler (an nvidia-smi sample
+        # every 200 ms) sees the timed region several times; rank 0's count for every rank
+        per_step = (time.perf_counter() - tw) / args.warmup
+        k = torch.tensor([min(2000, max(5, math.ceil(1.0 / max(per_step, 1e-6))))], device=dev)
+        if dist:
+            dist.broadcast(k, 0)
+        args.steps = int(k.item())
 
     def barrier():
         torch.cuda.synchronize()
