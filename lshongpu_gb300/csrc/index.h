@@ -145,7 +145,7 @@ void derive_simhash(Index& idx, cudaStream_t stream);
 
 // Persistence (persist.cpp): checksummed binary image of a built index.
 void save_index(const Index& idx, const char* path);
-std::unique_ptr<Index> load_index(const char* path, cudaStream_t stream);
+std::unique_ptr<Index> load_index(const char* path);  // owns a new stream
 
 }  // namespace lshg
 

@@ -379,8 +379,9 @@ void save_index(const Index& idx, const char* path) {
   fclose(f);
 }
 
-std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
-  // the whole file is read and its checksum compared before anything is parsed
+std::unique_ptr<Index> load_index(const char* path) {
+  // the whole file is read and its checksum compared before anything is parsed; no CUDA
+  // call is made before the file has passed every check
   std::vector<unsigned char> img;
   {
     FILE* f = fopen(path, "rb");
@@ -406,14 +407,17 @@ std::unique_ptr<Index> load_index(const char* path, cudaStream_t s) {
   scalars(r, I);
   read_ops(r, I.ops_keys);
   read_ops(r, I.ops_sketch);
-  buffers_io(r, I, s);
+  buffers_io(r, I, nullptr);  // staged in host memory only
   if (r.left != 0) throw Error(LSHG_ERR_IO, "corrupt index file (trailing bytes)");
   for (const auto* ops : {&I.ops_keys, &I.ops_sketch})
     for (const auto& op : *ops) need(op.kind == PrepOp::NORMALIZE || op.minv.size() == (size_t)I.d, "shift");
   check_loaded(r, I);
 
   // device work only from here on
+  cudaStream_t s;
+  LSHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   I.stream = s;
+  I.own_stream = true;
   cudaGetDevice(&I.device);
   I.p.opt.stream = nullptr;  // a stream handle of the process that saved the index
   if (I.p.framework == 1) I.lsh_grid = lsh_query_grid(1 << 30);  // this device's resident CTAs
@@ -448,16 +452,7 @@ int lshg_index_save(lshg_index* idx, const char* path) {
 int lshg_index_load(const char* path, lshg_index** out) {
   if (!path || !out) return LSHG_ERR_INVALID_ARGUMENT;
   try {
-    cudaStream_t s;
-    LSHG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    std::unique_ptr<Index> idx;
-    try {
-      idx = load_index(path, s);
-    } catch (...) {
-      cudaStreamDestroy(s);
-      throw;
-    }
-    idx->own_stream = true;
+    std::unique_ptr<Index> idx = load_index(path);
     auto* h = new lshg_index();
     h->impl = std::move(idx);
     *out = h;

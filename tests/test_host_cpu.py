@@ -130,6 +130,40 @@ def test_text_reader_matches_reference_reader(engine, tmp_path):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), i
 
 
+def _fnv1a64(data: bytes) -> bytes:
+    h = 1469598103934665603
+    for b in data:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    return h.to_bytes(8, "little")
+
+
+def test_damaged_index_files_refused_before_device_work(engine, tmp_path):
+    """lshg_index_load reads the whole file, compares its checksum and parses and checks
+    every field before its first CUDA call: on this GPU-less host each damaged file is
+    refused with LSHG_ERR_IO (a CUDA call would have failed with LSHG_ERR_CUDA first)."""
+    magic = b"LSHGIDX4"
+    body = magic + bytes(range(256)) * 4
+    cases = {
+        "missing": None,
+        "truncated": magic[:5],
+        "magic": b"NOTANIDX" + bytes(64) + _fnv1a64(b"NOTANIDX" + bytes(64)),
+        "checksum": body + b"\0" * 8,
+        # checksum right, contents not an index: the parser refuses it
+        "contents": body + _fnv1a64(body),
+        "zeros": magic + bytes(4096) + _fnv1a64(magic + bytes(4096)),
+    }
+    expect = {"missing": "cannot open", "truncated": "truncated", "magic": "not an lshg index",
+              "checksum": "checksum mismatch", "contents": "corrupt index file", "zeros": "corrupt index file"}
+    for name, data in cases.items():
+        p = tmp_path / f"{name}.lshg"
+        if data is not None:
+            p.write_bytes(data)
+        with pytest.raises(engine.LshgError) as e:
+            engine.Index.load(str(p))
+        assert e.value.status == 9, (name, str(e.value))  # LSHG_ERR_IO
+        assert expect[name] in str(e.value), (name, str(e.value))
+
+
 def _free_port():
     s = socket.socket()
     s.bind(("127.0.0.1", 0))
